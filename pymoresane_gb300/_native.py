@@ -1,0 +1,70 @@
+"""ctypes binding of libmsn.so (declared in include/msn.h).
+
+The library is loaded from the package directory; there is no fallback: if it
+is missing or CUDA is unavailable every entry point raises.
+"""
+import ctypes
+import os
+import threading
+
+_LIB = None
+_LOCK = threading.Lock()
+LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "libmsn.so")
+
+c_int, c_size_t, c_void_p, c_float, c_double = (ctypes.c_int, ctypes.c_size_t, ctypes.c_void_p,
+                                                ctypes.c_float, ctypes.c_double)
+
+# name -> (restype, [argtypes]); kept in the order of include/msn.h.
+SIGNATURES = {
+    "msn_last_error": (ctypes.c_char_p, []),
+    "msn_version": (c_int, []),
+    "msn_iuwt_workspace_bytes": (c_size_t, [c_int, c_int]),
+    "msn_iuwt_decompose": (c_int, [c_void_p, c_void_p, c_void_p, c_int, c_int, c_int, c_int, c_void_p, c_size_t,
+                                   c_void_p]),
+    "msn_iuwt_recompose": (c_int, [c_void_p, c_int, c_void_p, c_void_p, c_int, c_int, c_int, c_void_p, c_size_t,
+                                   c_void_p]),
+}
+
+
+class MsnError(RuntimeError):
+    """A libmsn entry point returned a non-zero status."""
+
+    def __init__(self, fn, code, msg):
+        super().__init__(f"{fn} failed with status {code}: {msg}")
+        self.code = code
+
+
+def load():
+    """Load libmsn.so once and declare every entry point's signature."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    with _LOCK:
+        if _LIB is None:
+            if not os.path.exists(LIB_PATH):
+                raise RuntimeError(
+                    f"libmsn.so not found at {LIB_PATH}; build it first with "
+                    "`python -m pymoresane_gb300.build` (the GPU path has no CPU fallback)")
+            lib = ctypes.CDLL(LIB_PATH)
+            for name, (res, args) in SIGNATURES.items():
+                fn = getattr(lib, name)
+                fn.restype = res
+                fn.argtypes = args
+            _LIB = lib
+    return _LIB
+
+
+def call(name, *args):
+    """Invoke entry point ``name``; raise MsnError on a non-zero status."""
+    lib = load()
+    rc = getattr(lib, name)(*args)
+    if rc != 0:
+        msg = lib.msn_last_error().decode(errors="replace")
+        if rc == -1:
+            raise ValueError(f"{name}: {msg}")
+        raise MsnError(name, rc, msg)
+    return rc
+
+
+def query(name, *args):
+    return getattr(load(), name)(*args)

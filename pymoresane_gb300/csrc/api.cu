@@ -1,0 +1,31 @@
+// libmsn: error reporting and version query.
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+
+#include "msn_common.cuh"
+
+namespace msn {
+
+static thread_local char g_last_error[512] = "";
+
+int set_error(int code, const char *fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_last_error, sizeof(g_last_error), fmt, ap);
+    va_end(ap);
+    return code;
+}
+
+void clear_error() { g_last_error[0] = '\0'; }
+
+int check_cuda(cudaError_t e, const char *what) {
+    if (e == cudaSuccess) return MSN_OK;
+    return set_error(MSN_ERR_CUDA, "%s: %s (%s)", what, cudaGetErrorString(e), cudaGetErrorName(e));
+}
+
+}  // namespace msn
+
+extern "C" const char *msn_last_error(void) { return msn::g_last_error; }
+
+extern "C" int msn_version(void) { return 100; }

@@ -1,0 +1,275 @@
+// Isotropic undecimated wavelet transform (a trous, B3 spline) for sm_103a.
+//
+// One kernel launch performs one complete separable smoothing at dilation d:
+// a CTA owns a band of full-width rows; the axis-0 (vertical) pass reads the
+// five taps straight from global memory with float4 loads (the taps of one
+// output row are whole rows r, r +- d, r +- 2d, mirrored at the borders) and
+// leaves the band in shared memory; the axis-1 (horizontal) pass then runs
+// entirely out of shared memory, so any dilation up to the row length is
+// handled without a horizontal halo. The epilogue optionally fuses the
+// wavelet detail (w = C_s - smooth(C_{s+1})) or the recomposition add
+// (rec = smooth(rec) + w), so no separate elementwise pass is ever launched.
+//
+// Arithmetic follows the reference's pyCUDA kernels bit for bit: FP32, centre
+// product then four fused multiply-adds, axis 0 before axis 1
+// (pymoresane/iuwt.py:588-659), detail as a rounded subtraction
+// (pymoresane/iuwt.py:403-417) and the recomposition add as a rounded addition
+// (pymoresane/iuwt.py:562).
+#include <mutex>
+
+#include "msn_common.cuh"
+
+namespace msn {
+namespace {
+
+enum Epilogue { kStore = 0, kDetail = 1, kAdd = 2 };
+
+constexpr int kThreads = 256;
+constexpr int kMaxSmem = 200 * 1024;
+
+template <int EPI>
+__global__ void __launch_bounds__(kThreads)
+atrous_band(const float *__restrict__ in, float *__restrict__ out, const float *__restrict__ aux,
+            int ny, int nx, int d, int band_rows) {
+    extern __shared__ float4 smem4[];
+    const float *band = reinterpret_cast<const float *>(smem4);
+    const int r0 = blockIdx.x * band_rows;
+    const int rows = min(band_rows, ny - r0);
+    const int nx4 = nx >> 2;
+    const float4 *in4 = reinterpret_cast<const float4 *>(in);
+
+    // Axis 0: out(r, c) = sum_k f_k * in(mirror(r + k d), c).
+    for (int i = threadIdx.x; i < rows * nx4; i += kThreads) {
+        const int rr = i / nx4;
+        const int c4 = i - rr * nx4;
+        const int r = r0 + rr;
+        const float4 xc = __ldg(in4 + (size_t)r * nx4 + c4);
+        const float4 a = __ldg(in4 + (size_t)mirror(r - 2 * d, ny) * nx4 + c4);
+        const float4 b = __ldg(in4 + (size_t)mirror(r - d, ny) * nx4 + c4);
+        const float4 e = __ldg(in4 + (size_t)mirror(r + d, ny) * nx4 + c4);
+        const float4 f = __ldg(in4 + (size_t)mirror(r + 2 * d, ny) * nx4 + c4);
+        float4 v;
+        v.x = b3_tap(xc.x, a.x, b.x, e.x, f.x);
+        v.y = b3_tap(xc.y, a.y, b.y, e.y, f.y);
+        v.z = b3_tap(xc.z, a.z, b.z, e.z, f.z);
+        v.w = b3_tap(xc.w, a.w, b.w, e.w, f.w);
+        smem4[i] = v;
+    }
+    __syncthreads();
+
+    // Axis 1 out of shared memory, with the fused epilogue.
+    for (int i = threadIdx.x; i < rows * nx; i += kThreads) {
+        const int rr = i / nx;
+        const int c = i - rr * nx;
+        const float *s = band + rr * nx;
+        float v = b3_tap(s[c], s[mirror(c - 2 * d, nx)], s[mirror(c - d, nx)], s[mirror(c + d, nx)],
+                         s[mirror(c + 2 * d, nx)]);
+        const size_t g = (size_t)(r0 + rr) * nx + c;
+        if (EPI == kDetail) v = __fsub_rn(__ldg(aux + g), v);
+        if (EPI == kAdd) v = __fadd_rn(v, __ldg(aux + g));
+        out[g] = v;
+    }
+}
+
+// rec = 0 + w: the first recomposition step when no smoothed plane is given
+// (the smoothing of an all-zero plane is exactly +0, and +0 + w maps -0 to +0
+// exactly as the reference's addition does).
+__global__ void zero_plus(const float4 *__restrict__ w, float4 *__restrict__ out, size_t n4) {
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n4; i += (size_t)gridDim.x * blockDim.x) {
+        float4 v = __ldg(w + i);
+        v.x = __fadd_rn(0.0f, v.x);
+        v.y = __fadd_rn(0.0f, v.y);
+        v.z = __fadd_rn(0.0f, v.z);
+        v.w = __fadd_rn(0.0f, v.w);
+        out[i] = v;
+    }
+}
+
+int band_rows_for(int ny, int nx) {
+    int band = ny / 304;                       // aim for >= 2 CTAs per SM on 152 SMs
+    band = band < 1 ? 1 : (band > 8 ? 8 : band);
+    const int smem_rows = (96 * 1024) / (nx * 4);
+    if (band > smem_rows) band = smem_rows < 1 ? 1 : smem_rows;
+    return band;
+}
+
+template <int EPI>
+int launch_band(const float *in, float *out, const float *aux, int ny, int nx, int d, cudaStream_t st) {
+    static std::once_flag once;
+    std::call_once(once, [] {
+        cudaFuncSetAttribute(atrous_band<EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxSmem);
+    });
+    const int band = band_rows_for(ny, nx);
+    const size_t smem = (size_t)band * nx * sizeof(float);
+    const int grid = (ny + band - 1) / band;
+    atrous_band<EPI><<<grid, kThreads, smem, st>>>(in, out, aux, ny, nx, d, band);
+    return check_launch("atrous_band");
+}
+
+int launch_zero_plus(const float *w, float *out, size_t n, cudaStream_t st) {
+    const size_t n4 = n / 4;
+    int grid = (int)((n4 + kThreads - 1) / kThreads);
+    if (grid > 152 * 16) grid = 152 * 16;
+    zero_plus<<<grid, kThreads, 0, st>>>(reinterpret_cast<const float4 *>(w), reinterpret_cast<float4 *>(out), n4);
+    return check_launch("zero_plus");
+}
+
+size_t plane_stride_bytes(int ny, int nx) { return (((size_t)ny * nx * sizeof(float)) + 255) & ~(size_t)255; }
+
+int validate_image(int ny, int nx, const char *fn) {
+    if (ny <= 0 || nx <= 0) return set_error(MSN_ERR_INVALID, "%s: empty image (%d x %d)", fn, ny, nx);
+    if (nx % 4 != 0) return set_error(MSN_ERR_INVALID, "%s: nx=%d must be a multiple of 4", fn, nx);
+    if ((size_t)nx * 4 > (size_t)kMaxSmem)
+        return set_error(MSN_ERR_INVALID, "%s: nx=%d exceeds the supported row length", fn, nx);
+    return MSN_OK;
+}
+
+int validate_scales(int ny, int nx, int top_scale, const char *fn) {
+    // Scales 0 .. top_scale-1 are used; the mirror needs 2^(s+1) <= n.
+    if (top_scale < 0 || top_scale > 30) return set_error(MSN_ERR_INVALID, "%s: bad scale count %d", fn, top_scale);
+    const long long span = 1LL << top_scale;
+    if (top_scale > 0 && (span > ny || span > nx))
+        return set_error(MSN_ERR_INVALID, "%s: 2^%d exceeds the image side (%d x %d)", fn, top_scale, ny, nx);
+    return MSN_OK;
+}
+
+}  // namespace
+
+// Smoothing entry points shared with the other translation units.
+int iuwt_smooth(const float *in, float *out, int ny, int nx, int scale, cudaStream_t st) {
+    return launch_band<kStore>(in, out, nullptr, ny, nx, 1 << scale, st);
+}
+int iuwt_smooth_detail(const float *in, const float *c0, float *w, int ny, int nx, int scale, cudaStream_t st) {
+    return launch_band<kDetail>(in, w, c0, ny, nx, 1 << scale, st);
+}
+int iuwt_smooth_add(const float *in, const float *w, float *out, int ny, int nx, int scale, cudaStream_t st) {
+    return launch_band<kAdd>(in, out, w, ny, nx, 1 << scale, st);
+}
+
+int iuwt_decompose_impl(const float *d_in, float *d_detail, float *d_smoothed, int ny, int nx, int scale_count,
+                        int scale_adjust, float *p0, float *p1, cudaStream_t st) {
+    const size_t plane = (size_t)ny * nx;
+    float *bufs[2] = {p0, p1};
+    const float *cur = d_in;
+    int cur_buf = -1;
+    auto next = [&]() { return cur_buf == 0 ? 1 : 0; };
+    for (int s = 0; s < scale_adjust; ++s) {
+        const int nb = next();
+        MSN_TRY(iuwt_smooth(cur, bufs[nb], ny, nx, s, st));
+        cur = bufs[nb];
+        cur_buf = nb;
+    }
+    for (int s = scale_adjust; s < scale_count; ++s) {
+        const bool last = (s == scale_count - 1);
+        const int nb = next();
+        float *c = (last && d_smoothed) ? d_smoothed : bufs[nb];
+        MSN_TRY(iuwt_smooth(cur, c, ny, nx, s, st));
+        MSN_TRY(iuwt_smooth_detail(c, cur, d_detail + (size_t)(s - scale_adjust) * plane, ny, nx, s, st));
+        cur = c;
+        cur_buf = (c == d_smoothed) ? -1 : nb;
+    }
+    if (d_smoothed && cur != d_smoothed) {
+        MSN_TRY(check_cuda(cudaMemcpyAsync(d_smoothed, cur, plane * sizeof(float), cudaMemcpyDeviceToDevice, st),
+                           "copy smoothed plane"));
+    }
+    return MSN_OK;
+}
+
+int iuwt_recompose_impl(const float *d_detail, int planes, const float *d_smoothed, float *d_out, int ny, int nx,
+                        int scale_adjust, float *p0, float *p1, cudaStream_t st) {
+    const size_t plane = (size_t)ny * nx;
+    float *bufs[2] = {p0, p1};
+    const int max_scale = planes + scale_adjust;
+    const int total = planes + scale_adjust;
+    const float *cur = d_smoothed;
+    int cur_buf = -1, op = 0;
+    auto dst_for = [&](int &nb) -> float * {
+        nb = (cur_buf == 0) ? 1 : 0;
+        return (op == total - 1) ? d_out : bufs[nb];
+    };
+    for (int s = max_scale - 1; s >= scale_adjust; --s, ++op) {
+        int nb;
+        float *dst = dst_for(nb);
+        const float *w = d_detail + (size_t)(s - scale_adjust) * plane;
+        if (cur == nullptr) {
+            MSN_TRY(launch_zero_plus(w, dst, plane, st));
+        } else {
+            MSN_TRY(iuwt_smooth_add(cur, w, dst, ny, nx, s, st));
+        }
+        cur = dst;
+        cur_buf = (dst == d_out) ? -1 : nb;
+    }
+    for (int s = scale_adjust - 1; s >= 0; --s, ++op) {
+        int nb;
+        float *dst = dst_for(nb);
+        if (cur == nullptr) {
+            MSN_TRY(check_cuda(cudaMemsetAsync(dst, 0, plane * sizeof(float), st), "zero plane"));
+        } else {
+            MSN_TRY(iuwt_smooth(cur, dst, ny, nx, s, st));
+        }
+        cur = dst;
+        cur_buf = (dst == d_out) ? -1 : nb;
+    }
+    if (total == 0) {
+        if (d_smoothed) {
+            MSN_TRY(check_cuda(cudaMemcpyAsync(d_out, d_smoothed, plane * sizeof(float), cudaMemcpyDeviceToDevice, st),
+                               "copy smoothed plane"));
+        } else {
+            MSN_TRY(check_cuda(cudaMemsetAsync(d_out, 0, plane * sizeof(float), st), "zero plane"));
+        }
+    }
+    return MSN_OK;
+}
+
+int split_workspace(void *d_work, size_t work_bytes, int ny, int nx, float **p0, float **p1, const char *fn) {
+    const size_t need = msn_iuwt_workspace_bytes(ny, nx);
+    if (d_work == nullptr || work_bytes < need)
+        return set_error(MSN_ERR_WORKSPACE, "%s: workspace of %zu bytes given, %zu needed", fn, work_bytes, need);
+    if (!aligned16(d_work)) return set_error(MSN_ERR_INVALID, "%s: workspace not 16-byte aligned", fn);
+    *p0 = reinterpret_cast<float *>(d_work);
+    *p1 = reinterpret_cast<float *>(reinterpret_cast<char *>(d_work) + plane_stride_bytes(ny, nx));
+    return MSN_OK;
+}
+
+}  // namespace msn
+
+using namespace msn;
+
+extern "C" size_t msn_iuwt_workspace_bytes(int ny, int nx) {
+    if (ny <= 0 || nx <= 0) return 0;
+    return 2 * plane_stride_bytes(ny, nx);
+}
+
+extern "C" int msn_iuwt_decompose(const float *d_in, float *d_detail, float *d_smoothed, int ny, int nx,
+                                  int scale_count, int scale_adjust, void *d_work, size_t work_bytes, void *stream) {
+    clear_error();
+    static const char *fn = "msn_iuwt_decompose";
+    MSN_TRY(validate_image(ny, nx, fn));
+    MSN_TRY(validate_scales(ny, nx, scale_count, fn));
+    if (scale_adjust < 0 || scale_adjust > scale_count)
+        return set_error(MSN_ERR_INVALID, "%s: scale_adjust=%d outside [0, %d]", fn, scale_adjust, scale_count);
+    if (!d_in || (scale_count > scale_adjust && !d_detail))
+        return set_error(MSN_ERR_INVALID, "%s: null input or detail pointer", fn);
+    if (!aligned16(d_in) || !aligned16(d_detail) || !aligned16(d_smoothed))
+        return set_error(MSN_ERR_INVALID, "%s: device pointers must be 16-byte aligned", fn);
+    float *p0, *p1;
+    MSN_TRY(split_workspace(d_work, work_bytes, ny, nx, &p0, &p1, fn));
+    return iuwt_decompose_impl(d_in, d_detail, d_smoothed, ny, nx, scale_count, scale_adjust, p0, p1,
+                               as_stream(stream));
+}
+
+extern "C" int msn_iuwt_recompose(const float *d_detail, int planes, const float *d_smoothed, float *d_out, int ny,
+                                  int nx, int scale_adjust, void *d_work, size_t work_bytes, void *stream) {
+    clear_error();
+    static const char *fn = "msn_iuwt_recompose";
+    MSN_TRY(validate_image(ny, nx, fn));
+    if (planes < 0 || scale_adjust < 0) return set_error(MSN_ERR_INVALID, "%s: negative plane count / adjust", fn);
+    MSN_TRY(validate_scales(ny, nx, planes + scale_adjust, fn));
+    if (!d_out || (planes > 0 && !d_detail)) return set_error(MSN_ERR_INVALID, "%s: null detail or output", fn);
+    if (!aligned16(d_detail) || !aligned16(d_smoothed) || !aligned16(d_out))
+        return set_error(MSN_ERR_INVALID, "%s: device pointers must be 16-byte aligned", fn);
+    float *p0, *p1;
+    MSN_TRY(split_workspace(d_work, work_bytes, ny, nx, &p0, &p1, fn));
+    return iuwt_recompose_impl(d_detail, planes, d_smoothed, d_out, ny, nx, scale_adjust, p0, p1,
+                               as_stream(stream));
+}

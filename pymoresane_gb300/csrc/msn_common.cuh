@@ -1,0 +1,56 @@
+// Shared helpers for libmsn: status handling and small device utilities.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stddef.h>
+
+#include "msn.h"
+
+namespace msn {
+
+// Records a formatted message as the calling thread's last error and returns
+// `code`.
+int set_error(int code, const char *fmt, ...);
+void clear_error();
+
+// Checks the result of a CUDA runtime call / kernel launch.
+int check_cuda(cudaError_t e, const char *what);
+
+inline int check_launch(const char *what) { return check_cuda(cudaGetLastError(), what); }
+
+inline cudaStream_t as_stream(void *s) { return reinterpret_cast<cudaStream_t>(s); }
+
+inline bool aligned16(const void *p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
+
+// B3 spline taps [1, 4, 6, 4, 1] / 16 (all exact in float32).
+constexpr float kB3Outer = 0.0625f;
+constexpr float kB3Inner = 0.25f;
+constexpr float kB3Centre = 0.375f;
+
+// Half-sample-symmetric mirror of index i into [0, n): x[-k] = x[k-1],
+// x[n-1+k] = x[n-k]. Valid for -n <= i < 2n.
+__device__ __forceinline__ int mirror(int i, int n) {
+    i = (i < 0) ? (-i - 1) : i;
+    i = (i >= n) ? (2 * n - i - 1) : i;
+    return i;
+}
+
+// One 5-tap B3 smoothing sample in the reference kernels' rounding order:
+// centre product, then fused multiply-adds for the taps at -2d, -d, +d, +2d.
+__device__ __forceinline__ float b3_tap(float xc, float xm2, float xm1, float xp1, float xp2) {
+    float acc = __fmul_rn(kB3Centre, xc);
+    acc = __fmaf_rn(kB3Outer, xm2, acc);
+    acc = __fmaf_rn(kB3Inner, xm1, acc);
+    acc = __fmaf_rn(kB3Inner, xp1, acc);
+    acc = __fmaf_rn(kB3Outer, xp2, acc);
+    return acc;
+}
+
+}  // namespace msn
+
+#define MSN_TRY(expr)                 \
+    do {                              \
+        int _msn_rc = (expr);         \
+        if (_msn_rc != MSN_OK) return _msn_rc; \
+    } while (0)
