@@ -70,6 +70,59 @@ int msn_iuwt_recompose(const float *d_detail, int planes, const float *d_smoothe
                        int ny, int nx, int scale_adjust, void *d_work, size_t work_bytes,
                        void *stream);
 
+/* ---------------------------------------------------------------------------
+ * Real 2-D FFTs and the PSF convolution (square grids, side m = 2^a in
+ * [32, 8192] or 3 * 2^a in [24, 6144]; complex data is interleaved float2,
+ * i.e. complex64)
+ * ------------------------------------------------------------------------- */
+
+/* Scratch bytes for msn_fft_convolve(n, m) and for msn_rfft2 / msn_irfft2 /
+ * msn_psf_spectrum at grid side m. */
+size_t msn_fft_workspace_bytes(int n, int m);
+
+/* Number of complex64 elements of a packed PSF spectrum for grid side m. */
+size_t msn_spectrum_elems(int m);
+
+/* Packed spectrum (library layout, consumed by msn_fft_convolve) of a real
+ * rows x cols PSF block placed at (off_r, off_c) in an m x m zero grid, i.e.
+ * rfft2 of that grid. Replaces the PSF-spectrum set-up of
+ * DataImage.moresane, pymoresane/main.py:135-213 (gpu_r2c_fft of the PSF or
+ * of pad_array(PSF)). */
+int msn_psf_spectrum(const float *d_psf, int rows, int cols, int m, int off_r, int off_c, void *d_spec,
+                     void *d_work, size_t work_bytes, void *stream);
+
+/* Converts a standard-layout rfft2 spectrum [m][m/2+1] into the packed
+ * layout used by msn_fft_convolve. */
+int msn_spectrum_pack(const void *d_std, int m, void *d_packed, void *stream);
+
+/* Replaces fft_convolve(in1, in2, conv_device='gpu', conv_mode) --
+ * pymoresane/iuwt_convolution.py:18-61: x [n][n] convolved with the PSF whose
+ * packed spectrum is d_spec; linear != 0: m == 2n, result
+ * crop_centre(fftshift(irfft2(rfft2(pad(x)) * H))); linear == 0: m == n,
+ * result fftshift(irfft2(rfft2(x) * H)). d_out: [n][n]. */
+int msn_fft_convolve(const float *d_x, int n, int m, const void *d_spec, float *d_out, int linear, void *d_work,
+                     size_t work_bytes, void *stream);
+
+/* Replaces gpu_r2c_fft -- pymoresane/iuwt_convolution.py:76-106:
+ * d_out [m][m/2+1] = rfft2(d_in [m][m]). */
+int msn_rfft2(const float *d_in, int m, void *d_out, void *d_work, size_t work_bytes, void *stream);
+
+/* Replaces gpu_c2r_ifft (+ scale_fft) -- pymoresane/iuwt_convolution.py:108-139:
+ * d_out [m][m] = irfft2(d_in [m][m/2+1]) (divided by m^2). */
+int msn_irfft2(const void *d_in, int m, float *d_out, void *d_work, size_t work_bytes, void *stream);
+
+/* Replaces fft_shift -- pymoresane/iuwt_convolution.py:161-201: in-place
+ * quadrant swap of an even m x m image. */
+int msn_fft_shift(float *d_data, int m, void *stream);
+
+/* Replaces contiguous_slice -- pymoresane/iuwt_convolution.py:204-239:
+ * d_out [m/2][m/2] = d_in[m/4 : 3m/4, m/4 : 3m/4]. */
+int msn_crop_centre(const float *d_in, int m, float *d_out, void *stream);
+
+/* Replaces scale_fft -- pymoresane/iuwt_convolution.py:242-265:
+ * d_data[i] /= divisor for i < count. */
+int msn_scale(float *d_data, size_t count, float divisor, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -23,6 +23,17 @@ SIGNATURES = {
                                    c_void_p]),
     "msn_iuwt_recompose": (c_int, [c_void_p, c_int, c_void_p, c_void_p, c_int, c_int, c_int, c_void_p, c_size_t,
                                    c_void_p]),
+    "msn_fft_workspace_bytes": (c_size_t, [c_int, c_int]),
+    "msn_spectrum_elems": (c_size_t, [c_int]),
+    "msn_psf_spectrum": (c_int, [c_void_p, c_int, c_int, c_int, c_int, c_int, c_void_p, c_void_p, c_size_t,
+                                 c_void_p]),
+    "msn_spectrum_pack": (c_int, [c_void_p, c_int, c_void_p, c_void_p]),
+    "msn_fft_convolve": (c_int, [c_void_p, c_int, c_int, c_void_p, c_void_p, c_int, c_void_p, c_size_t, c_void_p]),
+    "msn_rfft2": (c_int, [c_void_p, c_int, c_void_p, c_void_p, c_size_t, c_void_p]),
+    "msn_irfft2": (c_int, [c_void_p, c_int, c_void_p, c_void_p, c_size_t, c_void_p]),
+    "msn_fft_shift": (c_int, [c_void_p, c_int, c_void_p]),
+    "msn_crop_centre": (c_int, [c_void_p, c_int, c_void_p, c_void_p]),
+    "msn_scale": (c_int, [c_void_p, c_size_t, c_float, c_void_p]),
 }
 
 

@@ -41,9 +41,32 @@ def _cuda_lib_dir():
     return os.path.join(home, "lib64")
 
 
+TWIDDLE_N = 24576  # 2^13 * 3: every supported FFT length divides it
+
+
+def write_twiddles():
+    """Generate msn_twiddles.inc: exp(-2 pi i k / TWIDDLE_N) rounded from float64 to float32.
+
+    Emitted as exact hexadecimal float literals; included by csrc/fft_core.cuh.
+    """
+    import numpy as np
+
+    path = os.path.join(BUILD, "msn_twiddles.inc")
+    k = np.arange(TWIDDLE_N, dtype=np.float64)
+    ang = -2.0 * np.pi * k / TWIDDLE_N
+    c = np.cos(ang).astype(np.float32)
+    s = np.sin(ang).astype(np.float32)
+    lines = [f"{{{float(a).hex()}f, {float(b).hex()}f}}," for a, b in zip(c, s)]
+    text = "\n".join(lines) + "\n"
+    if not os.path.exists(path) or open(path).read() != text:
+        with open(path, "w") as fh:
+            fh.write(text)
+    return path
+
+
 def _flags(extra=()):
-    return ["-O3", "-std=c++17", "-lineinfo", *ARCH, "-Xcompiler", "-fPIC,-O3", "-I", INCLUDE, "-I", CSRC,
-            "--expt-relaxed-constexpr", *extra]
+    return ["-O3", "-std=c++20", "-lineinfo", *ARCH, "-Xcompiler", "-fPIC,-O3", "-I", INCLUDE, "-I", CSRC,
+            "-I", BUILD, "--expt-relaxed-constexpr", *extra]
 
 
 def _run(cmd):
@@ -60,10 +83,12 @@ def sources():
 def build(verbose=False, extra_flags=(), force=False):
     """Compile every csrc/*.cu and link libmsn.so. Returns the library path."""
     os.makedirs(BUILD, exist_ok=True)
+    write_twiddles()
     nvcc = _nvcc()
     srcs = sources()
     headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h"))]
     headers += [os.path.join(INCLUDE, f) for f in os.listdir(INCLUDE)]
+    headers += [os.path.join(BUILD, "msn_twiddles.inc")]
     newest_header = max((os.path.getmtime(h) for h in headers), default=0.0)
 
     def compile_one(src):

@@ -27,6 +27,62 @@ enum Epilogue { kStore = 0, kDetail = 1, kAdd = 2 };
 constexpr int kThreads = 256;
 constexpr int kMaxSmem = 200 * 1024;
 
+__device__ __forceinline__ float4 b3_tap4(const float4 &xc, const float4 &a, const float4 &b, const float4 &e,
+                                          const float4 &f) {
+    float4 v;
+    v.x = b3_tap(xc.x, a.x, b.x, e.x, f.x);
+    v.y = b3_tap(xc.y, a.y, b.y, e.y, f.y);
+    v.z = b3_tap(xc.z, a.z, b.z, e.z, f.z);
+    v.w = b3_tap(xc.w, a.w, b.w, e.w, f.w);
+    return v;
+}
+
+struct Taps4 {
+    float4 c, a, b, e, f;
+};
+
+__device__ __forceinline__ Taps4 load_vertical(const float4 *__restrict__ in4, int r, int c4, int ny, int nx4, int d) {
+    Taps4 t;
+    t.c = __ldg(in4 + (size_t)r * nx4 + c4);
+    t.a = __ldg(in4 + (size_t)mirror(r - 2 * d, ny) * nx4 + c4);
+    t.b = __ldg(in4 + (size_t)mirror(r - d, ny) * nx4 + c4);
+    t.e = __ldg(in4 + (size_t)mirror(r + d, ny) * nx4 + c4);
+    t.f = __ldg(in4 + (size_t)mirror(r + 2 * d, ny) * nx4 + c4);
+    return t;
+}
+
+// Horizontal pass for the four outputs at columns c .. c+3 of one shared-memory row.
+__device__ __forceinline__ float4 horizontal4(const float *__restrict__ s, int c, int nx, int d) {
+    const float4 *s4 = reinterpret_cast<const float4 *>(s);
+    if (d <= 2 && c >= 4 && c + 8 <= nx) {
+        // Window s[c-4 .. c+8) from three aligned LDS.128 covers every tap for d = 1, 2.
+        const float4 w0 = s4[(c >> 2) - 1], w1 = s4[c >> 2], w2 = s4[(c >> 2) + 1];
+        float e[12] = {w0.x, w0.y, w0.z, w0.w, w1.x, w1.y, w1.z, w1.w, w2.x, w2.y, w2.z, w2.w};
+        float4 v;
+        float *vp = reinterpret_cast<float *>(&v);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const int m = 4 + k;
+            vp[k] = (d == 1) ? b3_tap(e[m], e[m - 2], e[m - 1], e[m + 1], e[m + 2])
+                             : b3_tap(e[m], e[m - 4], e[m - 2], e[m + 2], e[m + 4]);
+        }
+        return v;
+    }
+    if (d >= 4 && c - 2 * d >= 0 && c + 3 + 2 * d < nx) {
+        // Every tap offset is a multiple of 4: five aligned LDS.128.
+        return b3_tap4(s4[c >> 2], s4[(c - 2 * d) >> 2], s4[(c - d) >> 2], s4[(c + d) >> 2], s4[(c + 2 * d) >> 2]);
+    }
+    float4 v;
+    float *vp = reinterpret_cast<float *>(&v);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const int cc = c + k;
+        vp[k] = b3_tap(s[cc], s[mirror(cc - 2 * d, nx)], s[mirror(cc - d, nx)], s[mirror(cc + d, nx)],
+                       s[mirror(cc + 2 * d, nx)]);
+    }
+    return v;
+}
+
 template <int EPI>
 __global__ void __launch_bounds__(kThreads)
 atrous_band(const float *__restrict__ in, float *__restrict__ out, const float *__restrict__ aux,
@@ -36,38 +92,49 @@ atrous_band(const float *__restrict__ in, float *__restrict__ out, const float *
     const int r0 = blockIdx.x * band_rows;
     const int rows = min(band_rows, ny - r0);
     const int nx4 = nx >> 2;
+    const int total4 = rows * nx4;
     const float4 *in4 = reinterpret_cast<const float4 *>(in);
 
-    // Axis 0: out(r, c) = sum_k f_k * in(mirror(r + k d), c).
-    for (int i = threadIdx.x; i < rows * nx4; i += kThreads) {
+    // Axis 0: two float4 columns per thread per iteration keep ten loads in flight.
+    int i = threadIdx.x;
+    for (; i + kThreads < total4; i += 2 * kThreads) {
+        const int i2 = i + kThreads;
+        const int rr1 = i / nx4, rr2 = i2 / nx4;
+        const Taps4 t1 = load_vertical(in4, r0 + rr1, i - rr1 * nx4, ny, nx4, d);
+        const Taps4 t2 = load_vertical(in4, r0 + rr2, i2 - rr2 * nx4, ny, nx4, d);
+        smem4[i] = b3_tap4(t1.c, t1.a, t1.b, t1.e, t1.f);
+        smem4[i2] = b3_tap4(t2.c, t2.a, t2.b, t2.e, t2.f);
+    }
+    if (i < total4) {
         const int rr = i / nx4;
-        const int c4 = i - rr * nx4;
-        const int r = r0 + rr;
-        const float4 xc = __ldg(in4 + (size_t)r * nx4 + c4);
-        const float4 a = __ldg(in4 + (size_t)mirror(r - 2 * d, ny) * nx4 + c4);
-        const float4 b = __ldg(in4 + (size_t)mirror(r - d, ny) * nx4 + c4);
-        const float4 e = __ldg(in4 + (size_t)mirror(r + d, ny) * nx4 + c4);
-        const float4 f = __ldg(in4 + (size_t)mirror(r + 2 * d, ny) * nx4 + c4);
-        float4 v;
-        v.x = b3_tap(xc.x, a.x, b.x, e.x, f.x);
-        v.y = b3_tap(xc.y, a.y, b.y, e.y, f.y);
-        v.z = b3_tap(xc.z, a.z, b.z, e.z, f.z);
-        v.w = b3_tap(xc.w, a.w, b.w, e.w, f.w);
-        smem4[i] = v;
+        const Taps4 t = load_vertical(in4, r0 + rr, i - rr * nx4, ny, nx4, d);
+        smem4[i] = b3_tap4(t.c, t.a, t.b, t.e, t.f);
     }
     __syncthreads();
 
-    // Axis 1 out of shared memory, with the fused epilogue.
-    for (int i = threadIdx.x; i < rows * nx; i += kThreads) {
-        const int rr = i / nx;
-        const int c = i - rr * nx;
-        const float *s = band + rr * nx;
-        float v = b3_tap(s[c], s[mirror(c - 2 * d, nx)], s[mirror(c - d, nx)], s[mirror(c + d, nx)],
-                         s[mirror(c + 2 * d, nx)]);
-        const size_t g = (size_t)(r0 + rr) * nx + c;
-        if (EPI == kDetail) v = __fsub_rn(__ldg(aux + g), v);
-        if (EPI == kAdd) v = __fadd_rn(v, __ldg(aux + g));
-        out[g] = v;
+    // Axis 1 out of shared memory (four columns per thread), fused epilogue, float4 stores.
+    const float4 *aux4 = reinterpret_cast<const float4 *>(aux);
+    float4 *out4 = reinterpret_cast<float4 *>(out);
+    for (int j = threadIdx.x; j < total4; j += kThreads) {
+        const int rr = j / nx4;
+        const int c4 = j - rr * nx4;
+        const size_t g4 = (size_t)(r0 + rr) * nx4 + c4;
+        float4 x;
+        if (EPI != kStore) x = __ldg(aux4 + g4);
+        float4 v = horizontal4(band + rr * nx, c4 * 4, nx, d);
+        if (EPI == kDetail) {
+            v.x = __fsub_rn(x.x, v.x);
+            v.y = __fsub_rn(x.y, v.y);
+            v.z = __fsub_rn(x.z, v.z);
+            v.w = __fsub_rn(x.w, v.w);
+        }
+        if (EPI == kAdd) {
+            v.x = __fadd_rn(v.x, x.x);
+            v.y = __fadd_rn(v.y, x.y);
+            v.z = __fadd_rn(v.z, x.z);
+            v.w = __fadd_rn(v.w, x.w);
+        }
+        out4[g4] = v;
     }
 }
 
@@ -86,11 +153,13 @@ __global__ void zero_plus(const float4 *__restrict__ w, float4 *__restrict__ out
 }
 
 int band_rows_for(int ny, int nx) {
-    int band = ny / 304;                       // aim for >= 2 CTAs per SM on 152 SMs
-    band = band < 1 ? 1 : (band > 8 ? 8 : band);
-    const int smem_rows = (96 * 1024) / (nx * 4);
-    if (band > smem_rows) band = smem_rows < 1 ? 1 : smem_rows;
-    return band;
+    // Small bands: 8 KB of shared memory per 2048 columns keeps many CTAs (and
+    // their loads) resident per SM; at least ~4 CTAs per SM overall.
+    int band = (32 * 1024) / (nx * 4);
+    const int by_grid = ny / (152 * 4);
+    if (band > by_grid) band = by_grid;
+    if (band > 8) band = 8;
+    return band < 1 ? 1 : band;
 }
 
 template <int EPI>

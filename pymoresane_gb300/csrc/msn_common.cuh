@@ -49,8 +49,8 @@ __device__ __forceinline__ float b3_tap(float xc, float xm2, float xm1, float xp
 
 }  // namespace msn
 
-#define MSN_TRY(expr)                 \
+#define MSN_TRY(...)                  \
     do {                              \
-        int _msn_rc = (expr);         \
+        int _msn_rc = (__VA_ARGS__);  \
         if (_msn_rc != MSN_OK) return _msn_rc; \
     } while (0)

@@ -83,3 +83,124 @@ def iuwt_recompose(w, scale_adjust=0, smoothed=None, out=None, work=None):
     _native.call("msn_iuwt_recompose", w.data_ptr() if planes > 0 else None, planes, _ptr(smoothed),
                  out.data_ptr(), ny, nx, scale_adjust, work.data_ptr(), work.numel(), stream_handle())
     return out
+
+
+# ---------------------------------------------------------------------------
+# FFTs and the PSF convolution
+# ---------------------------------------------------------------------------
+
+def fft_workspace(n, m, device):
+    nbytes = _native.query("msn_fft_workspace_bytes", n, m)
+    if nbytes == 0:
+        raise ValueError(f"unsupported FFT size m={m} (need 2^a in [32, 8192] or 3*2^a in [24, 6144])")
+    return torch.empty(nbytes, dtype=torch.uint8, device=device)
+
+
+class PsfSpectrum:
+    """rfft2 of a PSF on an m x m grid, held on the device in libmsn's packed layout."""
+
+    def __init__(self, packed, m):
+        self.packed = packed
+        self.m = m
+
+    @property
+    def device(self):
+        return self.packed.device
+
+
+def psf_spectrum(psf, m=None, off_r=None, off_c=None, work=None):
+    """Packed spectrum of ``psf`` placed at (off_r, off_c) (default: centred) in an m x m zero grid."""
+    psf = as_f32_cuda(psf)
+    rows, cols = psf.shape
+    m = rows if m is None else int(m)
+    off_r = (m - rows) // 2 if off_r is None else int(off_r)
+    off_c = (m - cols) // 2 if off_c is None else int(off_c)
+    elems = _native.query("msn_spectrum_elems", m)
+    if elems == 0:
+        raise ValueError(f"unsupported FFT size m={m}")
+    packed = torch.empty(elems, dtype=torch.complex64, device=psf.device)
+    if work is None:
+        work = fft_workspace(m, m, psf.device)
+    _native.call("msn_psf_spectrum", psf.data_ptr(), rows, cols, m, off_r, off_c, packed.data_ptr(),
+                 work.data_ptr(), work.numel(), stream_handle())
+    return PsfSpectrum(packed, m)
+
+
+def pack_spectrum(spec):
+    """Convert a standard rfft2 spectrum [m, m/2+1] (torch or numpy) into a PsfSpectrum."""
+    require_cuda()
+    if isinstance(spec, PsfSpectrum):
+        return spec
+    t = spec if isinstance(spec, torch.Tensor) else torch.as_tensor(spec)
+    t = t.to(device="cuda", dtype=torch.complex64).contiguous()
+    if t.dim() != 2 or t.shape[1] != t.shape[0] // 2 + 1:
+        raise ValueError("a PSF spectrum must have shape [m, m/2 + 1]")
+    m = t.shape[0]
+    elems = _native.query("msn_spectrum_elems", m)
+    if elems == 0:
+        raise ValueError(f"unsupported FFT size m={m}")
+    packed = torch.empty(elems, dtype=torch.complex64, device=t.device)
+    _native.call("msn_spectrum_pack", t.data_ptr(), m, packed.data_ptr(), stream_handle())
+    return PsfSpectrum(packed, m)
+
+
+def fft_convolve(x, spec, linear=True, out=None, work=None):
+    """Convolution of the n x n image ``x`` with the PSF of ``spec`` (linear: m == 2n, circular: m == n)."""
+    x = as_f32_cuda(x)
+    spec = pack_spectrum(spec)
+    n = x.shape[0]
+    if x.dim() != 2 or x.shape[1] != n:
+        raise ValueError("fft_convolve expects a square image")
+    if out is None:
+        out = torch.empty((n, n), dtype=torch.float32, device=x.device)
+    if work is None:
+        work = fft_workspace(n, spec.m, x.device)
+    _native.call("msn_fft_convolve", x.data_ptr(), n, spec.m, spec.packed.data_ptr(), out.data_ptr(),
+                 1 if linear else 0, work.data_ptr(), work.numel(), stream_handle())
+    return out
+
+
+def rfft2(x, work=None):
+    x = as_f32_cuda(x)
+    m = x.shape[0]
+    if x.dim() != 2 or x.shape[1] != m:
+        raise ValueError("rfft2 expects a square image")
+    out = torch.empty((m, m // 2 + 1), dtype=torch.complex64, device=x.device)
+    if work is None:
+        work = fft_workspace(m, m, x.device)
+    _native.call("msn_rfft2", x.data_ptr(), m, out.data_ptr(), work.data_ptr(), work.numel(), stream_handle())
+    return out
+
+
+def irfft2(spec, work=None):
+    require_cuda()
+    t = spec if isinstance(spec, torch.Tensor) else torch.as_tensor(spec)
+    t = t.to(device="cuda", dtype=torch.complex64).contiguous()
+    m = t.shape[0]
+    if t.dim() != 2 or t.shape[1] != m // 2 + 1:
+        raise ValueError("irfft2 expects a spectrum of shape [m, m/2 + 1]")
+    out = torch.empty((m, m), dtype=torch.float32, device=t.device)
+    if work is None:
+        work = fft_workspace(m, m, t.device)
+    _native.call("msn_irfft2", t.data_ptr(), m, out.data_ptr(), work.data_ptr(), work.numel(), stream_handle())
+    return out
+
+
+def fft_shift_(x):
+    x = as_f32_cuda(x)
+    _native.call("msn_fft_shift", x.data_ptr(), x.shape[0], stream_handle())
+    return x
+
+
+def crop_centre(x):
+    x = as_f32_cuda(x)
+    m = x.shape[0]
+    out = torch.empty((m // 2, m // 2), dtype=torch.float32, device=x.device)
+    _native.call("msn_crop_centre", x.data_ptr(), m, out.data_ptr(), stream_handle())
+    return out
+
+
+def scale_(x, divisor):
+    x = as_f32_cuda(x)
+    _native.call("msn_scale", x.data_ptr(), x.numel(), float(divisor), stream_handle())
+    return x

@@ -50,7 +50,22 @@ def gen_iuwt(ref):
     save("iuwt", **out)
 
 
-GENERATORS = {"iuwt": gen_iuwt}
+def gen_conv(ref):
+    from pymoresane_gb300.synthetic import make_psf
+    rng = np.random.default_rng(99)
+    x = rng.standard_normal((64, 64)).astype(np.float32)
+    psf2 = make_psf(128, 400, np.random.default_rng(5))
+    psf1 = make_psf(64, 200, np.random.default_rng(6))
+    h2 = np.fft.rfft2(psf2)
+    h1 = np.fft.rfft2(psf1)
+    conv = ref.iuwt_convolution
+    save("conv", x=x, psf2=psf2, psf1=psf1,
+         linear=conv.fft_convolve(x, h2, "cpu", "linear"),
+         circular=conv.fft_convolve(x, h1, "cpu", "circular"),
+         pad=conv.pad_array(x))
+
+
+GENERATORS = {"iuwt": gen_iuwt, "conv": gen_conv}
 
 
 def main():
