@@ -123,6 +123,98 @@ int msn_crop_centre(const float *d_in, int m, float *d_out, void *stream);
  * d_data[i] /= divisor for i < count. */
 int msn_scale(float *d_data, size_t count, float divisor, void *stream);
 
+/* ---------------------------------------------------------------------------
+ * Noise estimate, thresholding, labelling, source extraction
+ * ------------------------------------------------------------------------- */
+
+/* Scratch bytes for msn_mad_sigma / msn_source_extraction / msn_label on
+ * `planes` planes of ny x nx. */
+size_t msn_toolbox_workspace_bytes(int planes, int ny, int nx);
+
+/* Replaces estimate_threshold(in1, edge_excl, int_excl) --
+ * pymoresane/iuwt_toolbox.py:17-48: d_sigma[p] (float64 holding the float32
+ * result, as the reference's float64 output array does) = median(|w_p| over
+ * the pixel set) / 0.6745 (exact median; float32 mean of the two middle
+ * values for even counts, float32 division). rects[8] = {y0, y1, x0, x1, ey0, ey1, ex0, ex1}: pixels in
+ * [y0,y1) x [x0,x1) and not in [ey0,ey1) x [ex0,ex1) (host array). */
+int msn_mad_sigma(const float *d_w, int planes, int ny, int nx, const int *rects, double *d_sigma, void *d_work,
+                  size_t work_bytes, void *stream);
+
+/* Replaces apply_threshold(in1, threshold, sigma_level) --
+ * pymoresane/iuwt_toolbox.py:50-75 -- fused with the edge-suppression
+ * product (pymoresane/main.py:292-293; d_supp_rects [planes][4] = {y0, y1,
+ * x0, x1} kept region, or NULL) and the per-plane maximum used for the
+ * normalised scale maxima (pymoresane/main.py:297-300; d_plane_max or NULL;
+ * then d_work needs planes * 4 bytes). d_sigma: float64 [planes] (device);
+ * the comparison |w| > sigma_level * sigma is made in float64. */
+int msn_apply_threshold(const float *d_w, int planes, int ny, int nx, const double *d_sigma, double sigma_level,
+                        const int *d_supp_rects, float *d_out, float *d_plane_max, void *d_work, size_t work_bytes,
+                        void *stream);
+
+/* Replaces source_extraction(in1, tolerance, mode='gpu', neg_comp) --
+ * pymoresane/iuwt_toolbox.py:77-95 -> gpu_source_extraction :156-290.
+ * d_mask (float32 0/1) and d_extracted (= mask * w, may be NULL) are
+ * [planes][ny][nx]. */
+int msn_source_extraction(const float *d_w, int planes, int ny, int nx, float tolerance, int neg_comp, float *d_mask,
+                          float *d_extracted, void *d_work, size_t work_bytes, void *stream);
+
+/* 8-connected labelling of d_img != 0 with scipy.ndimage.label numbering (the
+ * labelling used by pymoresane/iuwt_toolbox.py:130,235). d_labels int32
+ * [ny][nx]; d_count (device int, may be NULL) receives the label count. */
+int msn_label(const float *d_img, int ny, int nx, int *d_labels, int *d_count, void *d_work, size_t work_bytes,
+              void *stream);
+
+/* ---------------------------------------------------------------------------
+ * CG minor loop / major loop vector work (float64 reductions, deterministic)
+ * Scalar block d_scal (float64): [0] r.r  [1] p.Ap  [2] alpha  [3] rn.rn  [4] beta
+ * ------------------------------------------------------------------------- */
+
+/* Scratch bytes for every reduction below. */
+size_t msn_reduce_workspace_bytes(void);
+
+/* d_out2[0] = sum a*b, d_out2[1] = sum c*d (c, d may both be NULL) in float64
+ * (np.dot at pymoresane/main.py:386-387,407-408). */
+int msn_dot2(const float *d_a, const float *d_b, const float *d_c, const float *d_d, size_t n, double *d_out2,
+             void *d_work, size_t work_bytes, void *stream);
+
+/* d_out2[0] = sum a^2, d_out2[1] = sum (a - b)^2 in float64: the norms of
+ * snr_ratio, pymoresane/iuwt_toolbox.py:292-306. */
+int msn_snr_sums(const float *d_a, const float *d_b, size_t n, double *d_out2, void *d_work, size_t work_bytes,
+                 void *stream);
+
+/* alpha = scal[0] / scal[1] -> scal[2]; xn = x + alpha p; *d_neg_count += #(xn < 0)
+ * (pymoresane/main.py:386-390). */
+int msn_cg_alpha_x(const float *d_x, const float *d_p, double *d_scal, float *d_xn, size_t n, int *d_neg_count,
+                   void *stream);
+
+/* xn[xn < 0] = 0; p = (xn - x) / alpha (pymoresane/main.py:394-397). */
+int msn_cg_positivity(const float *d_x, float *d_xn, float *d_p, const double *d_scal, size_t n, void *stream);
+
+/* rn = r - alpha Ap; scal[3] = rn.rn; scal[4] = beta = scal[3] / scal[0]
+ * (pymoresane/main.py:405-409). */
+int msn_cg_residual(const float *d_r, const float *d_ap, double *d_scal, float *d_rn, size_t n, void *d_work,
+                    size_t work_bytes, void *stream);
+
+/* p = rn + beta p (pymoresane/main.py:411). */
+int msn_cg_direction(const float *d_rn, float *d_p, const double *d_scal, size_t n, void *stream);
+
+/* model[off_r + i][off_c + j] += sign * gain * x[i][j] in float32
+ * (pymoresane/main.py:483,498); model has row pitch `pitch`. */
+int msn_model_update(float *d_model, int pitch, const float *d_x, int n_sub, int off_r, int off_c, float gain,
+                     int sign, void *stream);
+
+/* out = a - b (float32; pymoresane/main.py:485). */
+int msn_sub(const float *d_a, const float *d_b, float *d_out, size_t n, void *stream);
+
+/* out = a * b (float32; mask products, pymoresane/main.py:383,402,416). */
+int msn_mul(const float *d_a, const float *d_b, float *d_out, size_t n, void *stream);
+
+/* Mean and standard deviation (float64) of a rows x cols region of an image
+ * with row pitch `pitch` (np.std at pymoresane/main.py:490):
+ * d_out4 = {sum, sum of squared deviations, mean, std}. */
+int msn_region_std(const float *d_img, int pitch, int rows, int cols, int off_r, int off_c, double *d_out4,
+                   void *d_work, size_t work_bytes, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -34,6 +34,24 @@ SIGNATURES = {
     "msn_fft_shift": (c_int, [c_void_p, c_int, c_void_p]),
     "msn_crop_centre": (c_int, [c_void_p, c_int, c_void_p, c_void_p]),
     "msn_scale": (c_int, [c_void_p, c_size_t, c_float, c_void_p]),
+    "msn_toolbox_workspace_bytes": (c_size_t, [c_int, c_int, c_int]),
+    "msn_mad_sigma": (c_int, [c_void_p, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_size_t, c_void_p]),
+    "msn_apply_threshold": (c_int, [c_void_p, c_int, c_int, c_int, c_void_p, c_double, c_void_p, c_void_p, c_void_p,
+                                    c_void_p, c_size_t, c_void_p]),
+    "msn_source_extraction": (c_int, [c_void_p, c_int, c_int, c_int, c_float, c_int, c_void_p, c_void_p, c_void_p,
+                                      c_size_t, c_void_p]),
+    "msn_label": (c_int, [c_void_p, c_int, c_int, c_void_p, c_void_p, c_void_p, c_size_t, c_void_p]),
+    "msn_reduce_workspace_bytes": (c_size_t, []),
+    "msn_dot2": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_size_t, c_void_p, c_void_p, c_size_t, c_void_p]),
+    "msn_snr_sums": (c_int, [c_void_p, c_void_p, c_size_t, c_void_p, c_void_p, c_size_t, c_void_p]),
+    "msn_cg_alpha_x": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_size_t, c_void_p, c_void_p]),
+    "msn_cg_positivity": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_size_t, c_void_p]),
+    "msn_cg_residual": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_size_t, c_void_p, c_size_t, c_void_p]),
+    "msn_cg_direction": (c_int, [c_void_p, c_void_p, c_void_p, c_size_t, c_void_p]),
+    "msn_model_update": (c_int, [c_void_p, c_int, c_void_p, c_int, c_int, c_int, c_float, c_int, c_void_p]),
+    "msn_sub": (c_int, [c_void_p, c_void_p, c_void_p, c_size_t, c_void_p]),
+    "msn_mul": (c_int, [c_void_p, c_void_p, c_void_p, c_size_t, c_void_p]),
+    "msn_region_std": (c_int, [c_void_p, c_int, c_int, c_int, c_int, c_int, c_void_p, c_void_p, c_size_t, c_void_p]),
 }
 
 

@@ -1,0 +1,313 @@
+// Conjugate-gradient minor loop and major-loop vector work
+// (pymoresane/main.py:365-503) for sm_103a.
+//
+// Every inner product, the step sizes alpha / beta and the residual
+// statistics are accumulated in float64. Reductions are deterministic: a
+// fixed grid writes one float64 partial per CTA and a single CTA sums the
+// partials in a fixed order, so results are bit-identical run to run and do
+// not depend on what else shares the GPU. The CG scalars live in a small
+// device array (layout MSN_S_* in msn.h) so that the vector updates read
+// alpha and beta on the device and the host only needs the stop decisions.
+#include "msn_common.cuh"
+
+namespace msn {
+namespace {
+
+constexpr int kRedGrid = 4 * 152;
+constexpr int kRedThreads = 256;
+
+enum { S_RR = 0, S_PAP = 1, S_ALPHA = 2, S_RNRN = 3, S_BETA = 4 };
+
+__device__ __forceinline__ double block_sum(double v) {
+    __shared__ double sh[32];
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
+    __syncthreads();
+    const int nw = blockDim.x >> 5;
+    v = threadIdx.x < nw ? sh[threadIdx.x] : 0.0;
+    if (threadIdx.x < 32)
+        for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+    __syncthreads();
+    return v;  // valid in thread 0
+}
+
+// partials[2*b + 0] = sum a*b, partials[2*b + 1] = sum c*d (or sum (a - c)^2 when DIFF).
+template <bool DIFF>
+__global__ void __launch_bounds__(kRedThreads)
+dual_partials(const float *__restrict__ a, const float *__restrict__ b, const float *__restrict__ c,
+              const float *__restrict__ d, size_t n, double *__restrict__ partials) {
+    double s0 = 0.0, s1 = 0.0;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        s0 += (double)a[i] * (double)b[i];
+        if (DIFF) {
+            const double t = (double)a[i] - (double)c[i];
+            s1 += t * t;
+        } else if (c) {
+            s1 += (double)c[i] * (double)d[i];
+        }
+    }
+    s0 = block_sum(s0);
+    s1 = block_sum(s1);
+    if (threadIdx.x == 0) {
+        partials[2 * blockIdx.x] = s0;
+        partials[2 * blockIdx.x + 1] = s1;
+    }
+}
+
+// Sums the kRedGrid partial pairs in a fixed order into out[0], out[1].
+__global__ void __launch_bounds__(1024) finalize_pairs(const double *__restrict__ partials, double *__restrict__ out) {
+    __shared__ double s[2][1024];
+    const int t = threadIdx.x;
+    s[0][t] = t < kRedGrid ? partials[2 * t] : 0.0;
+    s[1][t] = t < kRedGrid ? partials[2 * t + 1] : 0.0;
+    __syncthreads();
+    for (int off = 512; off > 0; off >>= 1) {
+        if (t < off) {
+            s[0][t] += s[0][t + off];
+            s[1][t] += s[1][t + off];
+        }
+        __syncthreads();
+    }
+    if (t == 0) {
+        out[0] = s[0][0];
+        out[1] = s[1][0];
+    }
+}
+
+// xn = x + alpha p with alpha = rr / pAp (main.py:386-390); counts xn < 0.
+__global__ void cg_alpha_x(const float *__restrict__ x, const float *__restrict__ p, double *__restrict__ scal,
+                           float *__restrict__ xn, size_t n, int *__restrict__ neg) {
+    const double alpha = scal[S_RR] / scal[S_PAP];
+    if (blockIdx.x == 0 && threadIdx.x == 0) scal[S_ALPHA] = alpha;
+    int local = 0;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const float v = (float)((double)x[i] + alpha * (double)p[i]);
+        xn[i] = v;
+        local += v < 0.0f;
+    }
+    local = __reduce_add_sync(0xffffffffu, local);
+    if ((threadIdx.x & 31) == 0 && local) atomicAdd(neg, local);
+}
+
+// Positivity (main.py:394-397): xn[xn < 0] = 0; p = (xn - x) / alpha.
+__global__ void cg_positivity(const float *__restrict__ x, float *__restrict__ xn, float *__restrict__ p,
+                              const double *__restrict__ scal, size_t n) {
+    const double alpha = scal[S_ALPHA];
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        float v = xn[i];
+        if (v < 0.0f) v = 0.0f;
+        xn[i] = v;
+        p[i] = (float)(((double)v - (double)x[i]) / alpha);
+    }
+}
+
+// rn = r - alpha Ap with the per-CTA partial of rn . rn (main.py:405-408).
+__global__ void __launch_bounds__(kRedThreads)
+cg_residual(const float *__restrict__ r, const float *__restrict__ ap, const double *__restrict__ scal,
+            float *__restrict__ rn, size_t n, double *__restrict__ partials) {
+    const double alpha = scal[S_ALPHA];
+    double s = 0.0;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const float v = (float)((double)r[i] - alpha * (double)ap[i]);
+        rn[i] = v;
+        s += (double)v * (double)v;
+    }
+    s = block_sum(s);
+    if (threadIdx.x == 0) {
+        partials[2 * blockIdx.x] = s;
+        partials[2 * blockIdx.x + 1] = 0.0;
+    }
+}
+
+__global__ void cg_beta(double *__restrict__ scal) {
+    // beta = rn.rn / r.r (main.py:407-409); S_RNRN was written by finalize_pairs.
+    scal[S_BETA] = scal[S_RNRN] / scal[S_RR];
+}
+
+// p = rn + beta p (main.py:411).
+__global__ void cg_direction(const float *__restrict__ rn, float *__restrict__ p, const double *__restrict__ scal,
+                             size_t n) {
+    const double beta = scal[S_BETA];
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        p[i] = (float)((double)rn[i] + beta * (double)p[i]);
+}
+
+// model[sub] += sign * gain * x, in float32 as the reference does (main.py:483, 498).
+__global__ void model_update(float *__restrict__ model, int pitch, const float *__restrict__ x, int n_sub, int off_r,
+                             int off_c, float gain, float sign) {
+    const size_t total = (size_t)n_sub * n_sub;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+        const int r = (int)(i / n_sub), c = (int)(i - (size_t)r * n_sub);
+        float *m = model + (size_t)(r + off_r) * pitch + (c + off_c);
+        const float step = __fmul_rn(gain, x[i]);
+        *m = sign > 0.0f ? __fadd_rn(*m, step) : __fsub_rn(*m, step);
+    }
+}
+
+__global__ void sub_kernel(const float *__restrict__ a, const float *__restrict__ b, float *__restrict__ out, size_t n) {
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        out[i] = __fsub_rn(a[i], b[i]);
+}
+
+__global__ void mul_kernel(const float *__restrict__ a, const float *__restrict__ b, float *__restrict__ out, size_t n) {
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        out[i] = __fmul_rn(a[i], b[i]);
+}
+
+// Region sums for the standard deviation: pass 0 sums x, pass 1 sums (x - mean)^2.
+__global__ void __launch_bounds__(kRedThreads)
+region_partials(const float *__restrict__ img, int pitch, int rows, int cols, int off_r, int off_c,
+                const double *__restrict__ mean_in, double *__restrict__ partials) {
+    const double mean = mean_in ? mean_in[0] / ((double)rows * cols) : 0.0;
+    const size_t total = (size_t)rows * cols;
+    double s = 0.0;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+        const int r = (int)(i / cols), c = (int)(i - (size_t)r * cols);
+        const double v = (double)img[(size_t)(r + off_r) * pitch + c + off_c];
+        s += mean_in ? (v - mean) * (v - mean) : v;
+    }
+    s = block_sum(s);
+    if (threadIdx.x == 0) {
+        partials[2 * blockIdx.x] = s;
+        partials[2 * blockIdx.x + 1] = 0.0;
+    }
+}
+
+__global__ void std_finish(double *__restrict__ out2, long long count) {
+    // out2[0] = sum x, out2[1] = sum (x - mean)^2 -> out2[2] = mean, out2[3] = std
+    out2[2] = out2[0] / (double)count;
+    out2[3] = sqrt(out2[1] / (double)count);
+}
+
+int ew_grid(size_t n) {
+    size_t g = (n + 255) / 256;
+    if (g > 152 * 8) g = 152 * 8;
+    return g < 1 ? 1 : (int)g;
+}
+
+constexpr size_t kPartialBytes = 2 * kRedGrid * sizeof(double);
+
+}  // namespace
+
+int dual_reduce(const float *a, const float *b, const float *c, const float *d, size_t n, bool diff, double *out,
+                double *partials, cudaStream_t st) {
+    if (diff)
+        dual_partials<true><<<kRedGrid, kRedThreads, 0, st>>>(a, b, c, d, n, partials);
+    else
+        dual_partials<false><<<kRedGrid, kRedThreads, 0, st>>>(a, b, c, d, n, partials);
+    MSN_TRY(check_launch("dual_partials"));
+    finalize_pairs<<<1, 1024, 0, st>>>(partials, out);
+    return check_launch("finalize_pairs");
+}
+
+}  // namespace msn
+
+using namespace msn;
+
+extern "C" size_t msn_reduce_workspace_bytes(void) { return kPartialBytes; }
+
+static int check_red_ws(void *w, size_t b, const char *fn) {
+    if (!w || b < kPartialBytes) return set_error(MSN_ERR_WORKSPACE, "%s: workspace of %zu bytes needed", fn, kPartialBytes);
+    return MSN_OK;
+}
+
+extern "C" int msn_dot2(const float *d_a, const float *d_b, const float *d_c, const float *d_d, size_t n,
+                        double *d_out2, void *d_work, size_t work_bytes, void *stream) {
+    clear_error();
+    if (!d_a || !d_b || !d_out2 || ((d_c == nullptr) != (d_d == nullptr)))
+        return set_error(MSN_ERR_INVALID, "msn_dot2: null pointer");
+    MSN_TRY(check_red_ws(d_work, work_bytes, "msn_dot2"));
+    return dual_reduce(d_a, d_b, d_c, d_d, n, false, d_out2, (double *)d_work, as_stream(stream));
+}
+
+extern "C" int msn_snr_sums(const float *d_a, const float *d_b, size_t n, double *d_out2, void *d_work,
+                            size_t work_bytes, void *stream) {
+    clear_error();
+    if (!d_a || !d_b || !d_out2) return set_error(MSN_ERR_INVALID, "msn_snr_sums: null pointer");
+    MSN_TRY(check_red_ws(d_work, work_bytes, "msn_snr_sums"));
+    // out[0] = sum a^2, out[1] = sum (a - b)^2
+    return dual_reduce(d_a, d_a, d_b, nullptr, n, true, d_out2, (double *)d_work, as_stream(stream));
+}
+
+extern "C" int msn_cg_alpha_x(const float *d_x, const float *d_p, double *d_scal, float *d_xn, size_t n,
+                              int *d_neg_count, void *stream) {
+    clear_error();
+    if (!d_x || !d_p || !d_scal || !d_xn || !d_neg_count) return set_error(MSN_ERR_INVALID, "msn_cg_alpha_x: null pointer");
+    cg_alpha_x<<<ew_grid(n), 256, 0, as_stream(stream)>>>(d_x, d_p, d_scal, d_xn, n, d_neg_count);
+    return check_launch("cg_alpha_x");
+}
+
+extern "C" int msn_cg_positivity(const float *d_x, float *d_xn, float *d_p, const double *d_scal, size_t n,
+                                 void *stream) {
+    clear_error();
+    if (!d_x || !d_xn || !d_p || !d_scal) return set_error(MSN_ERR_INVALID, "msn_cg_positivity: null pointer");
+    cg_positivity<<<ew_grid(n), 256, 0, as_stream(stream)>>>(d_x, d_xn, d_p, d_scal, n);
+    return check_launch("cg_positivity");
+}
+
+extern "C" int msn_cg_residual(const float *d_r, const float *d_ap, double *d_scal, float *d_rn, size_t n,
+                               void *d_work, size_t work_bytes, void *stream) {
+    clear_error();
+    if (!d_r || !d_ap || !d_scal || !d_rn) return set_error(MSN_ERR_INVALID, "msn_cg_residual: null pointer");
+    MSN_TRY(check_red_ws(d_work, work_bytes, "msn_cg_residual"));
+    cudaStream_t st = as_stream(stream);
+    double *partials = (double *)d_work;
+    cg_residual<<<kRedGrid, kRedThreads, 0, st>>>(d_r, d_ap, d_scal, d_rn, n, partials);
+    MSN_TRY(check_launch("cg_residual"));
+    finalize_pairs<<<1, 1024, 0, st>>>(partials, d_scal + S_RNRN);   // writes S_RNRN and S_RNRN+1 (= S_BETA, overwritten next)
+    MSN_TRY(check_launch("finalize_pairs"));
+    cg_beta<<<1, 1, 0, st>>>(d_scal);
+    return check_launch("cg_beta");
+}
+
+extern "C" int msn_cg_direction(const float *d_rn, float *d_p, const double *d_scal, size_t n, void *stream) {
+    clear_error();
+    if (!d_rn || !d_p || !d_scal) return set_error(MSN_ERR_INVALID, "msn_cg_direction: null pointer");
+    cg_direction<<<ew_grid(n), 256, 0, as_stream(stream)>>>(d_rn, d_p, d_scal, n);
+    return check_launch("cg_direction");
+}
+
+extern "C" int msn_model_update(float *d_model, int pitch, const float *d_x, int n_sub, int off_r, int off_c,
+                                float gain, int sign, void *stream) {
+    clear_error();
+    if (!d_model || !d_x || n_sub <= 0 || off_r < 0 || off_c < 0 || off_c + n_sub > pitch)
+        return set_error(MSN_ERR_INVALID, "msn_model_update: bad arguments");
+    model_update<<<ew_grid((size_t)n_sub * n_sub), 256, 0, as_stream(stream)>>>(d_model, pitch, d_x, n_sub, off_r,
+                                                                                off_c, gain, sign >= 0 ? 1.0f : -1.0f);
+    return check_launch("model_update");
+}
+
+extern "C" int msn_sub(const float *d_a, const float *d_b, float *d_out, size_t n, void *stream) {
+    clear_error();
+    if (!d_a || !d_b || !d_out) return set_error(MSN_ERR_INVALID, "msn_sub: null pointer");
+    sub_kernel<<<ew_grid(n), 256, 0, as_stream(stream)>>>(d_a, d_b, d_out, n);
+    return check_launch("sub");
+}
+
+extern "C" int msn_mul(const float *d_a, const float *d_b, float *d_out, size_t n, void *stream) {
+    clear_error();
+    if (!d_a || !d_b || !d_out) return set_error(MSN_ERR_INVALID, "msn_mul: null pointer");
+    mul_kernel<<<ew_grid(n), 256, 0, as_stream(stream)>>>(d_a, d_b, d_out, n);
+    return check_launch("mul");
+}
+
+extern "C" int msn_region_std(const float *d_img, int pitch, int rows, int cols, int off_r, int off_c, double *d_out4,
+                              void *d_work, size_t work_bytes, void *stream) {
+    clear_error();
+    if (!d_img || !d_out4 || rows <= 0 || cols <= 0 || off_r < 0 || off_c < 0 || off_c + cols > pitch)
+        return set_error(MSN_ERR_INVALID, "msn_region_std: bad arguments");
+    MSN_TRY(check_red_ws(d_work, work_bytes, "msn_region_std"));
+    cudaStream_t st = as_stream(stream);
+    double *partials = (double *)d_work;
+    region_partials<<<kRedGrid, kRedThreads, 0, st>>>(d_img, pitch, rows, cols, off_r, off_c, nullptr, partials);
+    MSN_TRY(check_launch("region_partials"));
+    finalize_pairs<<<1, 1024, 0, st>>>(partials, d_out4);
+    MSN_TRY(check_launch("finalize_pairs"));
+    region_partials<<<kRedGrid, kRedThreads, 0, st>>>(d_img, pitch, rows, cols, off_r, off_c, d_out4, partials);
+    MSN_TRY(check_launch("region_partials"));
+    // keep the first sum: write the second pair to out[1] via a temporary slot
+    finalize_pairs<<<1, 1024, 0, st>>>(partials, d_out4 + 1);
+    MSN_TRY(check_launch("finalize_pairs"));
+    std_finish<<<1, 1, 0, st>>>(d_out4, (long long)rows * cols);
+    return check_launch("std_finish");
+}

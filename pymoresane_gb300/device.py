@@ -204,3 +204,134 @@ def scale_(x, divisor):
     x = as_f32_cuda(x)
     _native.call("msn_scale", x.data_ptr(), x.numel(), float(divisor), stream_handle())
     return x
+
+
+# ---------------------------------------------------------------------------
+# Noise estimate, thresholding, labelling, extraction
+# ---------------------------------------------------------------------------
+
+def toolbox_workspace(planes, ny, nx, device):
+    nbytes = _native.query("msn_toolbox_workspace_bytes", planes, ny, nx)
+    return torch.empty(max(nbytes, 16), dtype=torch.uint8, device=device)
+
+
+def noise_rects(ny, nx, edge_excl=0, int_excl=0):
+    """Pixel set of estimate_threshold as include / exclude rectangles.
+
+    Follows pymoresane/iuwt_toolbox.py:26-43 with Python slice semantics:
+    include [e:-e, e:-e] when edge_excl != 0 (else everything), exclude
+    [mid-i:mid+i, mid-i:mid+i] with mid = nx // 2 on both axes when int_excl != 0.
+    """
+    y0, y1, x0, x1 = 0, ny, 0, nx
+    ey0 = ey1 = ex0 = ex1 = 0
+    if edge_excl != 0:
+        y0, y1 = slice(edge_excl, -edge_excl).indices(ny)[:2]
+        x0, x1 = slice(edge_excl, -edge_excl).indices(nx)[:2]
+    if int_excl != 0:
+        mid = nx // 2
+        ey0, ey1 = slice(mid - int_excl, mid + int_excl).indices(ny)[:2]
+        ex0, ex1 = slice(mid - int_excl, mid + int_excl).indices(nx)[:2]
+    return (y0, y1, x0, x1, ey0, ey1, ex0, ex1)
+
+
+def mad_sigma(w, edge_excl=0, int_excl=0, out=None, work=None):
+    """Per-plane MAD noise estimate (float64 device tensor [planes])."""
+    import ctypes
+    w = as_f32_cuda(w)
+    if w.dim() == 2:
+        w = w.unsqueeze(0)
+    planes, ny, nx = w.shape
+    rects = (ctypes.c_int * 8)(*noise_rects(ny, nx, edge_excl, int_excl))
+    if out is None:
+        out = torch.empty(planes, dtype=torch.float64, device=w.device)
+    if work is None:
+        work = toolbox_workspace(planes, ny, nx, w.device)
+    _native.call("msn_mad_sigma", w.data_ptr(), planes, ny, nx, rects, out.data_ptr(), work.data_ptr(),
+                 work.numel(), stream_handle())
+    return out
+
+
+def apply_threshold(w, sigma, sigma_level=4, supp_rects=None, out=None, want_max=False, work=None):
+    """w * (|w| > sigma_level * sigma) per plane (+ optional suppression rectangles and plane maxima)."""
+    w = as_f32_cuda(w)
+    squeeze = w.dim() == 2
+    if squeeze:
+        w = w.unsqueeze(0)
+    planes, ny, nx = w.shape
+    if not isinstance(sigma, torch.Tensor) or sigma.dtype != torch.float64 or not sigma.is_cuda:
+        sigma = torch.as_tensor(sigma, dtype=torch.float64).reshape(-1).to(w.device)
+    if sigma.numel() == 1 and planes > 1:
+        sigma = sigma.expand(planes).contiguous()
+    if out is None:
+        out = torch.empty_like(w)
+    pmax = torch.empty(planes, dtype=torch.float32, device=w.device) if want_max else None
+    if work is None and want_max:
+        work = torch.empty(max(16, 4 * planes), dtype=torch.uint8, device=w.device)
+    _native.call("msn_apply_threshold", w.data_ptr(), planes, ny, nx, sigma.data_ptr(), float(sigma_level),
+                 _ptr(supp_rects), out.data_ptr(), _ptr(pmax), _ptr(work), 0 if work is None else work.numel(),
+                 stream_handle())
+    if squeeze:
+        out = out[0]
+    return (out, pmax) if want_max else out
+
+
+def source_extraction(w, tolerance, neg_comp=False, mask=None, extracted=None, work=None):
+    """Kept-island mask (float32 0/1) and mask * w for a coefficient stack."""
+    w = as_f32_cuda(w)
+    planes, ny, nx = w.shape
+    if mask is None:
+        mask = torch.empty_like(w)
+    if extracted is None:
+        extracted = torch.empty_like(w)
+    if work is None:
+        work = toolbox_workspace(planes, ny, nx, w.device)
+    _native.call("msn_source_extraction", w.data_ptr(), planes, ny, nx, float(tolerance), 1 if neg_comp else 0,
+                 mask.data_ptr(), extracted.data_ptr(), work.data_ptr(), work.numel(), stream_handle())
+    return mask, extracted
+
+
+def label(img, work=None):
+    """scipy.ndimage.label-compatible 8-connected labelling of img != 0: (int32 labels, count)."""
+    img = as_f32_cuda(img)
+    ny, nx = img.shape
+    labels = torch.empty((ny, nx), dtype=torch.int32, device=img.device)
+    count = torch.zeros(1, dtype=torch.int32, device=img.device)
+    if work is None:
+        work = toolbox_workspace(1, ny, nx, img.device)
+    _native.call("msn_label", img.data_ptr(), ny, nx, labels.data_ptr(), count.data_ptr(), work.data_ptr(),
+                 work.numel(), stream_handle())
+    return labels, int(count.item())
+
+
+# ---------------------------------------------------------------------------
+# Reductions and CG vector work
+# ---------------------------------------------------------------------------
+
+def reduce_workspace(device):
+    return torch.empty(_native.query("msn_reduce_workspace_bytes"), dtype=torch.uint8, device=device)
+
+
+def dot2(a, b, c=None, d=None, out=None, work=None):
+    out = torch.empty(2, dtype=torch.float64, device=a.device) if out is None else out
+    work = reduce_workspace(a.device) if work is None else work
+    _native.call("msn_dot2", a.data_ptr(), b.data_ptr(), _ptr(c), _ptr(d), a.numel(), out.data_ptr(),
+                 work.data_ptr(), work.numel(), stream_handle())
+    return out
+
+
+def snr_sums(a, b, out=None, work=None):
+    out = torch.empty(2, dtype=torch.float64, device=a.device) if out is None else out
+    work = reduce_workspace(a.device) if work is None else work
+    _native.call("msn_snr_sums", a.data_ptr(), b.data_ptr(), a.numel(), out.data_ptr(), work.data_ptr(),
+                 work.numel(), stream_handle())
+    return out
+
+
+def mul(a, b, out):
+    _native.call("msn_mul", a.data_ptr(), b.data_ptr(), out.data_ptr(), a.numel(), stream_handle())
+    return out
+
+
+def sub(a, b, out):
+    _native.call("msn_sub", a.data_ptr(), b.data_ptr(), out.data_ptr(), a.numel(), stream_handle())
+    return out

@@ -65,7 +65,28 @@ def gen_conv(ref):
          pad=conv.pad_array(x))
 
 
-GENERATORS = {"iuwt": gen_iuwt, "conv": gen_conv}
+def gen_toolbox(ref):
+    from pymoresane_gb300 import synthetic
+    dirty, psf, _ = synthetic.make_problem(synthetic.Workload(n=128, n_uv=800, n_points=12, n_gauss=2,
+                                                              sigma_range=(2.0, 5.0), noise=1e-2, seed=21))
+    tb = ref.iuwt_toolbox
+    d = ref.iuwt.iuwt_decomposition(dirty, 5, 0, "ser").astype(np.float32)
+    out = {"decomp": d}
+    for ee, ie in ((0, 0), (3, 0), (0, 5), (4, 7), (0, 70)):
+        out[f"thr_{ee}_{ie}"] = tb.estimate_threshold(d, ee, ie)
+    thr = out["thr_0_0"]
+    dt = tb.apply_threshold(d, thr, sigma_level=4)
+    out["thresh"] = dt
+    out["thresh_2d"] = tb.apply_threshold(d[1], thr[1], sigma_level=3)
+    for neg in (False, True):
+        src, msk = tb.source_extraction(dt[1:4], 0.75, mode="cpu", neg_comp=neg)
+        out[f"src_neg{int(neg)}"] = src
+        out[f"mask_neg{int(neg)}"] = msk
+    out["snr"] = np.array(tb.snr_ratio(dt[1:4].astype(np.float64), d[1:4]))
+    save("toolbox", **out)
+
+
+GENERATORS = {"iuwt": gen_iuwt, "conv": gen_conv, "toolbox": gen_toolbox}
 
 
 def main():

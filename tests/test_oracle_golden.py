@@ -63,3 +63,42 @@ def test_fma32_correctly_rounded():
         cands = [np.nextafter(r[i], np.float32(-np.inf)), r[i], np.nextafter(r[i], np.float32(np.inf))]
         errs = [abs(Fraction(float(v)) - exact) for v in cands]
         assert errs[1] <= min(errs)
+
+
+def test_convolution_oracle_bit_exact():
+    from oracle import convolution as C
+    g = load("conv")
+    assert np.array_equal(C.fft_convolve(g["x"], np.fft.rfft2(g["psf2"]), "linear"), g["linear"])
+    assert np.array_equal(C.fft_convolve(g["x"], np.fft.rfft2(g["psf1"]), "circular"), g["circular"])
+    assert np.array_equal(C.pad_array(g["x"]), g["pad"])
+
+
+@pytest.mark.parametrize("ee,ie", [(0, 0), (3, 0), (0, 5), (4, 7), (0, 70)])
+def test_estimate_threshold_bit_exact(ee, ie):
+    from oracle import toolbox as T
+    g = load("toolbox")
+    assert np.array_equal(T.estimate_threshold(g["decomp"], ee, ie), g[f"thr_{ee}_{ie}"])
+
+
+def test_apply_threshold_bit_exact():
+    from oracle import toolbox as T
+    g = load("toolbox")
+    d = g["decomp"]
+    got = T.apply_threshold(d, g["thr_0_0"], 4)
+    assert np.array_equal(got.view(np.uint32), g["thresh"].view(np.uint32))   # signed zeros included
+    assert np.array_equal(T.apply_threshold(d[1], g["thr_0_0"][1], 3), g["thresh_2d"])
+
+
+@pytest.mark.parametrize("neg", [0, 1])
+def test_source_extraction_bit_exact(neg):
+    from oracle import toolbox as T
+    g = load("toolbox")
+    src, msk = T.source_extraction(g["thresh"][1:4], 0.75, bool(neg), semantics="cpu")
+    assert src.dtype == np.float64 and msk.dtype == np.int32
+    assert np.array_equal(src, g[f"src_neg{neg}"]) and np.array_equal(msk, g[f"mask_neg{neg}"])
+
+
+def test_snr_ratio():
+    from oracle import toolbox as T
+    g = load("toolbox")
+    assert T.snr_ratio(g["thresh"][1:4].astype(np.float64), g["decomp"][1:4]) == float(g["snr"])
