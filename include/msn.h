@@ -158,6 +158,12 @@ int msn_apply_threshold(const float *d_w, int planes, int ny, int nx, const doub
 int msn_source_extraction(const float *d_w, int planes, int ny, int nx, float tolerance, int neg_comp, float *d_mask,
                           float *d_extracted, void *d_work, size_t work_bytes, void *stream);
 
+/* Per-plane maximum (of |w| when use_abs) as float32 [planes]; per_plane % 4
+ * == 0; d_work needs planes * 4 bytes (np.max at pymoresane/main.py:267 and
+ * iuwt_toolbox.py:127-129,232-234). */
+int msn_plane_max(const float *d_w, int planes, size_t per_plane, int use_abs, float *d_out, void *d_work,
+                  size_t work_bytes, void *stream);
+
 /* 8-connected labelling of d_img != 0 with scipy.ndimage.label numbering (the
  * labelling used by pymoresane/iuwt_toolbox.py:130,235). d_labels int32
  * [ny][nx]; d_count (device int, may be NULL) receives the label count. */
@@ -182,7 +188,7 @@ int msn_dot2(const float *d_a, const float *d_b, const float *d_c, const float *
 int msn_snr_sums(const float *d_a, const float *d_b, size_t n, double *d_out2, void *d_work, size_t work_bytes,
                  void *stream);
 
-/* alpha = scal[0] / scal[1] -> scal[2]; xn = x + alpha p; *d_neg_count += #(xn < 0)
+/* alpha = scal[0] / scal[1] -> scal[2]; xn = x + alpha p; *d_neg_count = #(xn < 0)
  * (pymoresane/main.py:386-390). */
 int msn_cg_alpha_x(const float *d_x, const float *d_p, double *d_scal, float *d_xn, size_t n, int *d_neg_count,
                    void *stream);

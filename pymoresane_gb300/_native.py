@@ -40,6 +40,7 @@ SIGNATURES = {
                                     c_void_p, c_size_t, c_void_p]),
     "msn_source_extraction": (c_int, [c_void_p, c_int, c_int, c_int, c_float, c_int, c_void_p, c_void_p, c_void_p,
                                       c_size_t, c_void_p]),
+    "msn_plane_max": (c_int, [c_void_p, c_int, c_size_t, c_int, c_void_p, c_void_p, c_size_t, c_void_p]),
     "msn_label": (c_int, [c_void_p, c_int, c_int, c_void_p, c_void_p, c_void_p, c_size_t, c_void_p]),
     "msn_reduce_workspace_bytes": (c_size_t, []),
     "msn_dot2": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_size_t, c_void_p, c_void_p, c_size_t, c_void_p]),

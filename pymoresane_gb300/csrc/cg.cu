@@ -81,7 +81,7 @@ __global__ void cg_alpha_x(const float *__restrict__ x, const float *__restrict_
     if (blockIdx.x == 0 && threadIdx.x == 0) scal[S_ALPHA] = alpha;
     int local = 0;
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-        const float v = (float)((double)x[i] + alpha * (double)p[i]);
+        const float v = (float)__dadd_rn((double)x[i], __dmul_rn(alpha, (double)p[i]));
         xn[i] = v;
         local += v < 0.0f;
     }
@@ -97,18 +97,22 @@ __global__ void cg_positivity(const float *__restrict__ x, float *__restrict__ x
         float v = xn[i];
         if (v < 0.0f) v = 0.0f;
         xn[i] = v;
-        p[i] = (float)(((double)v - (double)x[i]) / alpha);
+        p[i] = (float)__ddiv_rn(__dsub_rn((double)v, (double)x[i]), alpha);
     }
 }
 
 // rn = r - alpha Ap with the per-CTA partial of rn . rn (main.py:405-408).
+// The vector updates use explicitly rounded float64 products and sums (no
+// contraction into fused multiply-adds) so that they reproduce a float64
+// evaluation of the reference expressions exactly before the final rounding
+// to float32.
 __global__ void __launch_bounds__(kRedThreads)
 cg_residual(const float *__restrict__ r, const float *__restrict__ ap, const double *__restrict__ scal,
             float *__restrict__ rn, size_t n, double *__restrict__ partials) {
     const double alpha = scal[S_ALPHA];
     double s = 0.0;
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-        const float v = (float)((double)r[i] - alpha * (double)ap[i]);
+        const float v = (float)__dsub_rn((double)r[i], __dmul_rn(alpha, (double)ap[i]));
         rn[i] = v;
         s += (double)v * (double)v;
     }
@@ -129,7 +133,7 @@ __global__ void cg_direction(const float *__restrict__ rn, float *__restrict__ p
                              size_t n) {
     const double beta = scal[S_BETA];
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
-        p[i] = (float)((double)rn[i] + beta * (double)p[i]);
+        p[i] = (float)__dadd_rn((double)rn[i], __dmul_rn(beta, (double)p[i]));
 }
 
 // model[sub] += sign * gain * x, in float32 as the reference does (main.py:483, 498).
@@ -233,6 +237,7 @@ extern "C" int msn_cg_alpha_x(const float *d_x, const float *d_p, double *d_scal
                               int *d_neg_count, void *stream) {
     clear_error();
     if (!d_x || !d_p || !d_scal || !d_xn || !d_neg_count) return set_error(MSN_ERR_INVALID, "msn_cg_alpha_x: null pointer");
+    MSN_TRY(check_cuda(cudaMemsetAsync(d_neg_count, 0, sizeof(int), as_stream(stream)), "reset count"));
     cg_alpha_x<<<ew_grid(n), 256, 0, as_stream(stream)>>>(d_x, d_p, d_scal, d_xn, n, d_neg_count);
     return check_launch("cg_alpha_x");
 }

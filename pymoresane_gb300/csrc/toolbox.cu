@@ -607,6 +607,24 @@ extern "C" int msn_source_extraction(const float *d_w, int planes, int ny, int n
     return extraction_impl(d_w, planes, ny, nx, tolerance, neg_comp, d_mask, d_extracted, d_work, as_stream(stream));
 }
 
+extern "C" int msn_plane_max(const float *d_w, int planes, size_t per_plane, int use_abs, float *d_out, void *d_work,
+                             size_t work_bytes, void *stream) {
+    clear_error();
+    static const char *fn = "msn_plane_max";
+    if (!d_w || !d_out || planes <= 0 || per_plane == 0 || per_plane % 4)
+        return set_error(MSN_ERR_INVALID, "%s: bad arguments (plane size must be a positive multiple of 4)", fn);
+    if (!d_work || work_bytes < (size_t)planes * sizeof(int)) return set_error(MSN_ERR_WORKSPACE, "%s: workspace", fn);
+    cudaStream_t st = as_stream(stream);
+    int *enc = (int *)d_work;
+    init_max<<<(planes + 127) / 128, 128, 0, st>>>(enc, planes);
+    MSN_TRY(check_launch("init_max"));
+    plane_max_kernel<<<dim3(grid_for(per_plane / 4, 256, 4 * 152 / planes + 8), planes), 256, 0, st>>>(
+        d_w, per_plane / 4, use_abs, enc);
+    MSN_TRY(check_launch("plane_max"));
+    decode_max<<<(planes + 127) / 128, 128, 0, st>>>(enc, d_out, planes);
+    return check_launch("decode_max");
+}
+
 extern "C" int msn_label(const float *d_img, int ny, int nx, int *d_labels, int *d_count, void *d_work,
                          size_t work_bytes, void *stream) {
     clear_error();

@@ -335,3 +335,15 @@ def mul(a, b, out):
 def sub(a, b, out):
     _native.call("msn_sub", a.data_ptr(), b.data_ptr(), out.data_ptr(), a.numel(), stream_handle())
     return out
+
+
+def plane_max(w, use_abs=False, out=None, work=None):
+    """Per-plane maximum (float32 device tensor)."""
+    w = as_f32_cuda(w)
+    planes = 1 if w.dim() == 2 else w.shape[0]
+    per = w.numel() // planes
+    out = torch.empty(planes, dtype=torch.float32, device=w.device) if out is None else out
+    work = torch.empty(max(16, 4 * planes), dtype=torch.uint8, device=w.device) if work is None else work
+    _native.call("msn_plane_max", w.data_ptr(), planes, per, 1 if use_abs else 0, out.data_ptr(), work.data_ptr(),
+                 work.numel(), stream_handle())
+    return out

@@ -1,0 +1,477 @@
+"""Drop-in for pymoresane.main: DataImage / FitsImage with a device-resident MORESANE.
+
+The major loop (pymoresane/main.py:266-514), the conjugate-gradient minor
+loop (:378-457) and moresane_by_scale (:523-599) run with every image, PSF
+spectrum, coefficient stack, mask and CG vector resident on the GPU. Each
+step is a libmsn kernel (C ABI, include/msn.h); the host only reads back the
+scalars the reference's control flow branches on: the normalised scale
+maxima, the SNR of each minor iteration, the positivity flag, the residual
+standard deviation and the peak of the dirty subregion. The CG inner
+products and step sizes are float64, the bulk arithmetic float32.
+
+Signatures and defaults follow the reference except that the mode arguments
+default to the GPU path ('gpu'); CPU modes raise ValueError (this package
+has no CPU implementation). See INTEGRATION.md for every difference.
+"""
+import logging
+import math
+
+import numpy as np
+import torch
+
+from . import _native
+from . import device as dev
+from . import fits
+
+logger = logging.getLogger(__name__)
+
+
+def _check_modes(all_on_gpu, decom_mode, conv_device, extraction_mode):
+    if all_on_gpu:
+        return
+    bad = [f"{k}={v!r}" for k, v in (("decom_mode", decom_mode), ("conv_device", conv_device),
+                                     ("extraction_mode", extraction_mode)) if v != "gpu"]
+    if bad:
+        raise ValueError("pymoresane_gb300 implements the GPU path only; got " + ", ".join(bad)
+                         + " (use the 'gpu' modes or all_on_gpu=True)")
+
+
+def _rects_for(slc, n):
+    return slc.indices(n)[:2]
+
+
+class _PsfCache:
+    """PSF spectra and PSF scale energies, built once per (PSF, configuration) on the device."""
+
+    def __init__(self):
+        self.entries = {}
+
+    def get(self, key, build):
+        if key not in self.entries:
+            self.entries[key] = build()
+        return self.entries[key]
+
+
+class _Buffers:
+    """Per-(subregion, scale_count) device buffers reused across major iterations."""
+
+    def __init__(self, ns, n_full, m_sub, m_data, scale_count, device):
+        f32 = dict(dtype=torch.float32, device=device)
+        s = scale_count
+        self.dec = torch.empty((s, ns, ns), **f32)
+        self.thr = torch.empty((s, ns, ns), **f32)
+        self.emask = torch.empty((s, ns, ns), **f32)
+        self.esrc = torch.empty((s, ns, ns), **f32)
+        self.planes = torch.empty((s, ns, ns), **f32)
+        self.vec = {k: torch.empty((ns, ns), **f32) for k in ("x", "xn", "r", "rn", "p", "ap", "tmp", "rec")}
+        self.conv_full = torch.empty((n_full, n_full), **f32)
+        self.iuwt_work = dev.iuwt_workspace(ns, ns, device)
+        self.fft_work = dev.fft_workspace(ns, m_sub, device)
+        self.fft_work_full = dev.fft_workspace(n_full, m_data, device)
+        self.tool_work = dev.toolbox_workspace(s, ns, ns, device)
+        self.red_work = dev.reduce_workspace(device)
+        self.scal = torch.zeros(8, dtype=torch.float64, device=device)
+        self.snr2 = torch.zeros(2, dtype=torch.float64, device=device)
+        self.std4 = torch.zeros(4, dtype=torch.float64, device=device)
+        self.neg = torch.zeros(1, dtype=torch.int32, device=device)
+        self.small = torch.empty(256, dtype=torch.uint8, device=device)
+        self.fmax = torch.empty(1, dtype=torch.float32, device=device)
+
+
+class DataImage(object):
+    """MORESANE on one dirty image / PSF pair (pymoresane/main.py:18-676)."""
+
+    def __init__(self, dirty_data, psf_data, mask_data, cdelt1, cdelt2):
+        self.dirty_data = np.asarray(dirty_data).astype(np.float32)
+        self.psf_data = np.asarray(psf_data).astype(np.float32)
+        self.mask_name = None if mask_data is None else getattr(self, "mask_name", "mask")
+        self.mask = None if mask_data is None else np.asarray(mask_data)
+        self.dirty_data_shape = self.dirty_data.shape
+        self.psf_data_shape = self.psf_data.shape
+        self.complete = False
+        self.model = np.zeros_like(self.dirty_data)
+        self.residual = np.copy(self.dirty_data)
+        self.restored = np.zeros_like(self.dirty_data)
+        self.cdelt1 = cdelt1
+        self.cdelt2 = cdelt2
+        self.log = []
+        self._psf_cache = _PsfCache()
+        self._bufs = {}
+        self._dev = None
+
+    # ------------------------------------------------------------------ device state
+    def _device_inputs(self):
+        if self._dev is None:
+            dev.require_cuda()
+            _native.load()
+            d = torch.device("cuda", torch.cuda.current_device())
+            self._dev = {
+                "psf": torch.from_numpy(np.ascontiguousarray(self.psf_data)).to(d),
+                "mask": None if self.mask is None else torch.from_numpy(
+                    np.ascontiguousarray(self.mask, dtype=np.float32)).to(d),
+                "device": d,
+            }
+        return self._dev
+
+    def _spectra(self, subregion, conv_mode):
+        """(spec_sub, spec_data, psf_subregion) per pymoresane/main.py:118-213 (GPU branches)."""
+        devs = self._device_inputs()
+        psf = devs["psf"]
+        n = self.dirty_data_shape[0]
+        p0 = self.psf_data_shape[0]
+        double = all(p == 2 * d for p, d in zip(self.psf_data_shape, self.dirty_data_shape))
+        full = subregion == n
+
+        def crop(c, half):
+            return psf[c - half:c + half, c - half:c + half].contiguous()
+
+        def build():
+            if double:
+                psf_sub = crop(p0 // 2, subregion // 2)
+            else:
+                psf_sub = psf[n // 2 - subregion // 2:n // 2 + subregion // 2,
+                              n // 2 - subregion // 2:n // 2 + subregion // 2].contiguous()
+            if conv_mode == "circular":
+                spec_sub = dev.psf_spectrum(psf_sub, m=subregion)
+                if double:
+                    spec_data = dev.psf_spectrum(crop(p0 // 2, n // 2), m=n)
+                else:
+                    spec_data = spec_sub if subregion == p0 else dev.psf_spectrum(psf, m=p0)
+            elif conv_mode == "linear":
+                if double:
+                    if full:
+                        spec_sub = spec_data = dev.psf_spectrum(psf, m=p0)
+                    else:
+                        spec_sub = dev.psf_spectrum(crop(p0 // 2, subregion), m=2 * subregion)
+                        spec_data = dev.psf_spectrum(psf, m=p0)
+                else:
+                    if full:
+                        spec_sub = spec_data = dev.psf_spectrum(psf, m=2 * p0)   # rfft2(pad_array(psf))
+                    else:
+                        spec_sub = dev.psf_spectrum(crop(p0 // 2, subregion), m=2 * subregion)
+                        spec_data = dev.psf_spectrum(psf, m=2 * p0)
+            else:
+                raise ValueError(f"unknown conv_mode {conv_mode!r}")
+            return spec_sub, spec_data, psf_sub
+
+        return self._psf_cache.get((subregion, conv_mode), build)
+
+    def _energies(self, psf_sub, scale_count, bufs):
+        """||w_s||_2 of the PSF-subregion decomposition, as float32 (pymoresane/main.py:221-226)."""
+        def build():
+            ns = psf_sub.shape[0]
+            dec = torch.empty((scale_count, ns, ns), dtype=torch.float32, device=psf_sub.device)
+            dev.iuwt_decompose(psf_sub, scale_count, 0, out=dec, work=bufs.iuwt_work)
+            sums = torch.empty((scale_count, 2), dtype=torch.float64, device=psf_sub.device)
+            for s in range(scale_count):
+                dev.dot2(dec[s].reshape(-1), dec[s].reshape(-1), out=sums[s], work=bufs.red_work)
+            return np.sqrt(sums[:, 0].cpu().numpy()).astype(np.float32)
+        return self._psf_cache.get(("energies", psf_sub.data_ptr(), scale_count), build)
+
+    def _buffers(self, ns, scale_count, spec_sub, spec_data):
+        key = (ns, scale_count, spec_sub.m, spec_data.m)
+        if key not in self._bufs:
+            self._bufs = {key: _Buffers(ns, self.dirty_data_shape[0], spec_sub.m, spec_data.m, scale_count,
+                                        self._device_inputs()["device"])}
+        return self._bufs[key]
+
+    # ------------------------------------------------------------------ algorithm
+    def moresane(self, subregion=None, scale_count=None, sigma_level=4, loop_gain=0.1, tolerance=0.75, accuracy=1e-6,
+                 major_loop_miter=100, minor_loop_miter=30, all_on_gpu=False, decom_mode="gpu", core_count=1,
+                 conv_device='gpu', conv_mode='linear', extraction_mode='gpu', enforce_positivity=False,
+                 edge_suppression=False, edge_offset=0, flux_threshold=0, neg_comp=False, edge_excl=0, int_excl=0):
+        """MORESANE deconvolution (pymoresane/main.py:53-521); updates self.model and self.residual."""
+        _check_modes(all_on_gpu, decom_mode, conv_device, extraction_mode)
+        devs = self._device_inputs()
+        dirty = torch.from_numpy(np.ascontiguousarray(self.dirty_data)).to(devs["device"])
+        model, residual, major = self._moresane_device(
+            dirty, subregion, scale_count, sigma_level, loop_gain, tolerance, accuracy, major_loop_miter,
+            minor_loop_miter, conv_mode, enforce_positivity, edge_suppression, edge_offset, flux_threshold,
+            neg_comp, edge_excl, int_excl)
+        if major > 0:
+            self.model += model.cpu().numpy()
+            self.residual = residual.cpu().numpy()
+        return major
+
+    def moresane_by_scale(self, start_scale=1, stop_scale=20, subregion=None, sigma_level=4, loop_gain=0.1,
+                          tolerance=0.75, accuracy=1e-6, major_loop_miter=100, minor_loop_miter=30, all_on_gpu=False,
+                          decom_mode="gpu", core_count=1, conv_device='gpu', conv_mode='linear',
+                          extraction_mode='gpu', enforce_positivity=False, edge_suppression=False, edge_offset=0,
+                          flux_threshold=0, neg_comp=False, edge_excl=0, int_excl=0):
+        """Scale-by-scale MORESANE (pymoresane/main.py:523-599), residual kept on the device between scales."""
+        _check_modes(all_on_gpu, decom_mode, conv_device, extraction_mode)
+        devs = self._device_inputs()
+        d = devs["device"]
+        dirty = torch.from_numpy(np.ascontiguousarray(self.dirty_data)).to(d)
+        model_acc = torch.from_numpy(np.ascontiguousarray(self.model)).to(d)
+        residual = torch.from_numpy(np.ascontiguousarray(self.residual)).to(d)
+        n = self.dirty_data_shape[0]
+        st = dev.stream_handle()
+        scale_count = start_scale
+        self.complete = False
+        while not self.complete:
+            logger.info("MORESANE at scale %d", scale_count)
+            model, res, major = self._moresane_device(
+                dirty, subregion, scale_count, sigma_level, loop_gain, tolerance, accuracy, major_loop_miter,
+                minor_loop_miter, conv_mode, enforce_positivity, edge_suppression, edge_offset, flux_threshold,
+                neg_comp, edge_excl, int_excl)
+            if major > 0:
+                _native.call("msn_model_update", model_acc.data_ptr(), n, model.data_ptr(), n, 0, 0, 1.0, 1, st)
+                residual = res
+            dirty = residual
+            scale_count += 1
+            if scale_count > (np.log2(n)) - 1:
+                logger.info("Maximum scale reached - finished.")
+                break
+            if scale_count > stop_scale:
+                logger.info("Maximum scale reached - finished.")
+                break
+        self.model = model_acc.cpu().numpy()
+        self.residual = residual.cpu().numpy()
+        self.complete = False
+
+    def _moresane_device(self, dirty, subregion, scale_count, sigma_level, loop_gain, tolerance, accuracy,
+                         major_loop_miter, minor_loop_miter, conv_mode, enforce_positivity, edge_suppression,
+                         edge_offset, flux_threshold, neg_comp, edge_excl, int_excl):
+        n = self.dirty_data_shape[0]
+        if n % 2 == 1:
+            logger.error("Image size is uneven. Please use even dimensions.")
+            raise ValueError("Image size is uneven. Please use even dimensions.")
+        if subregion is None or subregion > n:
+            subregion = n
+        if scale_count is None or scale_count > (np.log2(n) - 1):
+            scale_count = int(np.log2(n) - 1)
+        ns = subregion
+        o = n // 2 - ns // 2
+        linear = conv_mode == "linear"
+        spec_sub, spec_data, psf_sub = self._spectra(subregion, conv_mode)
+        B = self._buffers(ns, scale_count, spec_sub, spec_data)
+        energies = self._energies(psf_sub, scale_count, B)
+        st = dev.stream_handle()
+        call = _native.call
+        V = B.vec
+        nvec = ns * ns
+        mask_sub = None
+        if self._dev["mask"] is not None:
+            mask_sub = self._dev["mask"][o:o + ns, o:o + ns].contiguous()
+
+        supp = None
+        if edge_suppression or edge_offset > 0:
+            rects = []
+            corruption = 0
+            for i in range(scale_count):
+                if edge_suppression:
+                    corruption += 2 * 2 ** i
+                    e = edge_offset if edge_offset > corruption else corruption
+                else:
+                    e = edge_offset
+                y0, y1 = _rects_for(slice(e, -e), ns)
+                rects.append([y0, y1, y0, y1])
+            supp = torch.tensor(rects, dtype=torch.int32, device=dirty.device)
+
+        def sub_view(img):
+            return img if ns == n else img[o:o + ns, o:o + ns].contiguous()
+
+        def apply_a(vec_in, vec_out, max_scale, adj, planes):
+            dev.fft_convolve(vec_in, spec_sub, linear, out=V["tmp"], work=B.fft_work)
+            w = B.planes[:planes]
+            dev.iuwt_decompose(V["tmp"], max_scale, adj, out=w, work=B.iuwt_work)
+            call("msn_mul", w.data_ptr(), B.emask.data_ptr(), w.data_ptr(), w.numel(), st)
+            dev.iuwt_recompose(w, adj, out=vec_out, work=B.iuwt_work)
+
+        def residual_of(model):
+            res = torch.empty((n, n), dtype=torch.float32, device=dirty.device)
+            dev.fft_convolve(model, spec_data, linear, out=B.conv_full, work=B.fft_work_full)
+            call("msn_sub", dirty.data_ptr(), B.conv_full.data_ptr(), res.data_ptr(), n * n, st)
+            return res
+
+        major = 0
+        max_coeff = 1
+        model = torch.zeros((n, n), dtype=torch.float32, device=dirty.device)
+        std_current, std_ratio = 1000, 1
+        min_scale = 0
+        residual = None
+        dirty_sub = sub_view(dirty)
+        normalised = None
+        have_x = False
+
+        def dirty_peak():
+            dev.plane_max(dirty_sub, out=B.fmax, work=B.small)
+            return float(B.fmax.item())
+
+        while (major < major_loop_miter and max_coeff > 0 and std_ratio > accuracy
+               and dirty_peak() > flux_threshold):
+            rec = {"major": major}
+            while min_scale < scale_count:
+                if min_scale == 0:
+                    dev.iuwt_decompose(dirty_sub, scale_count, 0, out=B.dec, work=B.iuwt_work)
+                    sigma = dev.mad_sigma(B.dec, edge_excl, int_excl, work=B.tool_work)
+                    if mask_sub is not None:
+                        masked = torch.empty_like(dirty_sub)
+                        call("msn_mul", dirty_sub.data_ptr(), mask_sub.data_ptr(), masked.data_ptr(), nvec, st)
+                        dev.iuwt_decompose(masked, scale_count, 0, out=B.dec, work=B.iuwt_work)
+                    _, pmax = dev.apply_threshold(B.dec, sigma, sigma_level, supp_rects=supp, out=B.thr,
+                                                  want_max=True, work=B.small)
+                    normalised = pmax.cpu().numpy() / energies
+                max_index = int(np.argmax(normalised[min_scale:])) + min_scale
+                max_scale = max_index + 1
+                max_coeff = normalised[max_index]
+                if max_coeff == 0:
+                    logger.info("No significant wavelet coefficients detected.")
+                    break
+                logger.info("Minimum scale = %d", min_scale)
+                logger.info("Maximum scale = %d", max_scale)
+                scale_adjust = 0
+                for i in range(max_index - 1, -1, -1):
+                    if normalised[i] == 0:
+                        scale_adjust = i + 1
+                        logger.info("Scale %d is empty. Ignoring scales <= %d", scale_adjust, scale_adjust)
+                        break
+                planes = max_scale - scale_adjust
+                thr = B.thr[scale_adjust:max_scale]
+                dev.source_extraction(thr, tolerance, neg_comp, mask=B.emask[:planes], extracted=B.esrc[:planes],
+                                      work=B.tool_work)
+                dev.iuwt_recompose(B.esrc[:planes], scale_adjust, out=V["rec"], work=B.iuwt_work)
+
+                x, xn, r, rn, p, ap = V["x"], V["xn"], V["r"], V["rn"], V["p"], V["ap"]
+                x.zero_()
+                r.copy_(V["rec"])
+                p.copy_(V["rec"])
+                minor = 0
+                snr_last = snr_current = 0.0
+                while minor < minor_loop_miter:
+                    apply_a(p, ap, max_scale, scale_adjust, planes)
+                    dev.dot2(r.reshape(-1), r.reshape(-1), p.reshape(-1), ap.reshape(-1), out=B.scal[0:2],
+                             work=B.red_work)
+                    call("msn_cg_alpha_x", x.data_ptr(), p.data_ptr(), B.scal.data_ptr(), xn.data_ptr(), nvec,
+                         B.neg.data_ptr(), st)
+                    if enforce_positivity and int(B.neg.item()) > 0:
+                        call("msn_cg_positivity", x.data_ptr(), xn.data_ptr(), p.data_ptr(), B.scal.data_ptr(),
+                             nvec, st)
+                        apply_a(p, ap, max_scale, scale_adjust, planes)
+                    call("msn_cg_residual", r.data_ptr(), ap.data_ptr(), B.scal.data_ptr(), rn.data_ptr(), nvec,
+                         B.red_work.data_ptr(), B.red_work.numel(), st)
+                    call("msn_cg_direction", rn.data_ptr(), p.data_ptr(), B.scal.data_ptr(), nvec, st)
+                    # model_sources = mask * W(H xn); snr against the extracted sources
+                    dev.fft_convolve(xn, spec_sub, linear, out=V["tmp"], work=B.fft_work)
+                    w = B.planes[:planes]
+                    dev.iuwt_decompose(V["tmp"], max_scale, scale_adjust, out=w, work=B.iuwt_work)
+                    call("msn_mul", w.data_ptr(), B.emask.data_ptr(), w.data_ptr(), w.numel(), st)
+                    dev.snr_sums(B.esrc[:planes].reshape(-1), w.reshape(-1), out=B.snr2, work=B.red_work)
+                    s2 = B.snr2.cpu().numpy()
+                    snr_last = snr_current
+                    with np.errstate(divide="ignore", invalid="ignore"):
+                        snr_current = float(20 * np.log10(np.sqrt(s2[0]) / np.sqrt(s2[1])))
+                    minor += 1
+                    logger.debug("SNR at iteration %d = %s", minor, snr_current)
+                    if minor == 1 and snr_current > 40:
+                        logger.info("SNR too large on first iteration - false detection. "
+                                    "Incrementing the minimum scale.")
+                        min_scale += 1
+                        break
+                    if snr_current > 40:
+                        logger.info("Model has reached <1% error - exiting minor loop.")
+                        V["x"], V["xn"] = xn, x
+                        x, xn = xn, x
+                        min_scale = 0
+                        break
+                    if minor > 2 and snr_current <= snr_last:
+                        if snr_current > 10.5:
+                            min_scale = 0
+                        else:
+                            min_scale += 1
+                        break
+                    V["r"], V["rn"] = rn, r
+                    r, rn = rn, r
+                    V["x"], V["xn"] = xn, x
+                    x, xn = xn, x
+                have_x = True
+                logger.info("%d minor loop iterations performed.", minor)
+                rec.update(max_scale=max_scale, scale_adjust=scale_adjust, minor=minor, snr=snr_current)
+                if minor == minor_loop_miter and snr_current > 10.5:
+                    min_scale = 0
+                    break
+                if min_scale == 0:
+                    break
+            if min_scale == scale_count:
+                logger.info("All scales are performing poorly - stopping.")
+                break
+            if max_coeff > 0 and have_x:
+                x = V["x"]
+                call("msn_model_update", model.data_ptr(), n, x.data_ptr(), ns, o, o, float(loop_gain), 1, st)
+                residual = residual_of(model)
+                std_last = std_current
+                call("msn_region_std", residual.data_ptr(), n, ns, ns, o, o, B.std4.data_ptr(),
+                     B.red_work.data_ptr(), B.red_work.numel(), st)
+                std_current = float(B.std4[3].item())
+                std_ratio = (std_last - std_current) / std_last
+                rec["std"] = std_current
+                rec["reverted"] = bool(std_ratio < 0)
+                if std_ratio < 0:
+                    logger.info("Residual has worsened - reverting changes.")
+                    call("msn_model_update", model.data_ptr(), n, x.data_ptr(), ns, o, o, float(loop_gain), -1, st)
+                    residual = residual_of(model)
+                dirty_sub = sub_view(residual)
+                major += 1
+                self.log.append(rec)
+                logger.info("%d major loop iterations performed.", major)
+            if major == 0:
+                logger.info("Current MORESANE iteration did no work - finished.")
+                self.complete = True
+                break
+        return model, residual, major
+
+    # ------------------------------------------------------------------ outputs
+    def save_fits(self, data, name):
+        data = np.asarray(data).reshape(1, 1, data.shape[0], data.shape[0])
+        fits.write(name, data, getattr(self, "img_hdr", None))
+
+    def make_logger(self, level="INFO"):
+        level = getattr(logging, level.upper())
+        lg = logging.getLogger(__name__)
+        lg.setLevel(logging.DEBUG)
+        fh = logging.FileHandler('PyMORESANE.log', mode='w')
+        fh.setLevel(level)
+        ch = logging.StreamHandler()
+        ch.setLevel(level)
+        fmt = logging.Formatter('%(asctime)s [%(levelname)s]: %(message)s', datefmt='[%m/%d/%Y] [%I:%M:%S]')
+        fh.setFormatter(fmt)
+        ch.setFormatter(fmt)
+        lg.addHandler(fh)
+        lg.addHandler(ch)
+        return lg
+
+
+class FitsImage(DataImage):
+    """DataImage read from FITS files (pymoresane/main.py:678-733), without astropy."""
+
+    def __init__(self, image_name, psf_name, mask_name=None):
+        self.image_name = image_name
+        self.psf_name = psf_name
+        self.mask_name = mask_name
+        img, self.img_hdr = fits.read(image_name)
+        psf, self.psf_hdr = fits.read(psf_name)
+        cdelt1 = self.psf_hdr['CDELT1']
+        cdelt2 = self.psf_hdr['CDELT1']   # the reference reads CDELT1 twice (main.py:704-705)
+        mask = None
+        if mask_name is not None:
+            from scipy.signal import fftconvolve
+            m, mhdr = fits.read(mask_name)
+            m = m[tuple(self.handle_input(mhdr))].astype(np.float64)
+            m = m / np.max(m)
+            m = fftconvolve(m, np.ones([5, 5]), mode="same")
+            mask = m / np.max(m)
+        super(FitsImage, self).__init__(dirty_data=img[tuple(self.handle_input(self.img_hdr))],
+                                        psf_data=psf[tuple(self.handle_input(self.psf_hdr))],
+                                        mask_data=mask, cdelt1=cdelt1, cdelt2=cdelt2)
+        self.mask_name = mask_name
+
+    def handle_input(self, input_hdr):
+        """Index selecting the RA/DEC plane of an N-D FITS cube (pymoresane/main.py:618-634)."""
+        input_slice = input_hdr['NAXIS'] * [0]
+        for i in range(input_hdr['NAXIS']):
+            if str(input_hdr.get('CTYPE%d' % (i + 1), "")).startswith("RA"):
+                input_slice[-1] = slice(None)
+            if str(input_hdr.get('CTYPE%d' % (i + 1), "")).startswith("DEC"):
+                input_slice[-2] = slice(None)
+        return input_slice

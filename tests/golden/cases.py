@@ -1,0 +1,28 @@
+"""Seeded MORESANE test cases shared by make_golden.py and the GPU tests.
+
+Each case is (problem kwargs, run kwargs); the problem is a synthetic dirty
+image / PSF pair (pymoresane_gb300.synthetic) and the run kwargs are passed
+to DataImage.moresane together with RUN_DEFAULTS.
+"""
+import numpy as np
+
+MORESANE_CASES = {
+    # name: (problem kwargs, run kwargs)
+    "lin_double": (dict(n=128, psf_factor=2, seed=31), dict(scale_count=4, conv_mode="linear")),
+    "circ_pos": (dict(n=128, psf_factor=1, seed=32), dict(scale_count=4, conv_mode="circular",
+                                                         enforce_positivity=True)),
+    "lin_same_edge": (dict(n=128, psf_factor=1, seed=33), dict(scale_count=4, conv_mode="linear",
+                                                              edge_suppression=True)),
+    "lin_subregion": (dict(n=128, psf_factor=2, seed=34), dict(scale_count=4, conv_mode="linear", subregion=64)),
+    "neg_excl": (dict(n=128, psf_factor=2, seed=35), dict(scale_count=5, conv_mode="linear", neg_comp=True,
+                                                         edge_excl=6, int_excl=10, edge_offset=3)),
+}
+RUN_DEFAULTS = dict(sigma_level=4, loop_gain=0.2, tolerance=0.75, accuracy=1e-6, major_loop_miter=12,
+                    minor_loop_miter=30)
+
+
+def problem(n, psf_factor, seed):
+    from pymoresane_gb300 import synthetic
+    w = synthetic.Workload(n=n, psf_factor=psf_factor, n_uv=int(3000 * (n / 512) ** 2 * psf_factor ** 2 / 4) + 200,
+                           n_points=10, n_gauss=2, sigma_range=(2.0, 5.0), noise=1e-3, seed=seed)
+    return synthetic.make_problem(w)

@@ -21,6 +21,7 @@ sys.path.insert(0, HERE)
 sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
 
 import refshim  # noqa: E402
+from cases import MORESANE_CASES, RUN_DEFAULTS, problem  # noqa: E402
 
 
 def save(name, **arrays):
@@ -86,7 +87,45 @@ def gen_toolbox(ref):
     save("toolbox", **out)
 
 
-GENERATORS = {"iuwt": gen_iuwt, "conv": gen_conv, "toolbox": gen_toolbox}
+def gen_moresane(ref):
+    out = {}
+    for name, (pk, rk) in MORESANE_CASES.items():
+        dirty, psf, _ = problem(**pk)
+        kw = dict(RUN_DEFAULTS, **rk)
+        kw.setdefault("subregion", dirty.shape[0])
+        img = ref.main.DataImage(dirty, psf, None, 1.0, 1.0)
+        img.moresane(**kw)
+        out[f"{name}_dirty"] = dirty
+        out[f"{name}_psf"] = psf
+        out[f"{name}_model"] = img.model
+        out[f"{name}_residual"] = img.residual
+        print(name, float(img.model.sum()), float(np.count_nonzero(img.model)), float(img.residual.std()))
+    save("moresane", **out)
+
+
+def read_fits(path):
+    raw = open(path, "rb").read()
+    hdr = raw[:2880].decode()
+    cards = {hdr[i:i + 8].strip(): hdr[i + 10:i + 80].split("/")[0].strip() for i in range(0, 2880, 80)}
+    n1, n2 = int(cards["NAXIS1"]), int(cards["NAXIS2"])
+    return np.frombuffer(raw[2880:2880 + 8 * n1 * n2], dtype=">f8").reshape(n2, n1).astype(np.float64)
+
+
+def gen_tart(ref):
+    root = os.path.join(refshim.REF_ROOT, "tests")
+    dirty = read_fits(os.path.join(root, "dirty_2017-10-15_20:33:35_UTC.fits"))
+    beam = read_fits(os.path.join(root, "beam_2017-10-15_20:33:35_UTC.fits"))
+    img = ref.main.DataImage(dirty, beam, None, 0.703125, 0.703125)
+    img.moresane_by_scale(1, 20, subregion=256, sigma_level=4, loop_gain=0.2, tolerance=0.75, accuracy=1e-6,
+                          major_loop_miter=100, minor_loop_miter=50, conv_mode="circular",
+                          enforce_positivity=True)
+    print("tart", float(img.model.sum()), float(img.model.max()), int(np.count_nonzero(img.model)),
+          float(img.residual.std()))
+    save("tart", model=img.model, residual=img.residual)
+
+
+GENERATORS = {"iuwt": gen_iuwt, "conv": gen_conv, "toolbox": gen_toolbox, "moresane": gen_moresane,
+              "tart": gen_tart}
 
 
 def main():
