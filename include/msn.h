@@ -70,6 +70,21 @@ int msn_iuwt_recompose(const float *d_detail, int planes, const float *d_smoothe
                        int ny, int nx, int scale_adjust, void *d_work, size_t work_bytes,
                        void *stream);
 
+/* Same result as msn_iuwt_decompose, but the two scratch planes come from a
+ * fixed device array inside libmsn.so instead of a caller workspace, so the
+ * call allocates nothing. No counterpart in the reference: it exists for
+ * callers that cannot allocate device memory themselves (a host pipeline whose
+ * own pool allocator owns the GPU, or a loop that must never call cudaMalloc).
+ * Limit: ny * nx <= 1,048,576 pixels (e.g. 1024 x 1024); larger images return
+ * MSN_ERR_INVALID. The array (8 MiB) is reserved on every GPU
+ * that loads the library until the process exits. The first call on each
+ * device resolves the array's device address (cudaGetSymbolAddress); make
+ * that first call before any stream capture. All calls share the one array:
+ * calls that can overlap on the GPU (different streams, or different host
+ * threads on the same device) race and must be serialised by the caller. */
+int msn_iuwt_decompose_static(const float *d_in, float *d_detail, float *d_smoothed, int ny, int nx,
+                              int scale_count, int scale_adjust, void *stream);
+
 /* ---------------------------------------------------------------------------
  * Real 2-D FFTs and the PSF convolution (square grids, side m = 2^a in
  * [32, 8192] or 3 * 2^a in [24, 6144]; complex data is interleaved float2,

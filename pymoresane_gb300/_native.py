@@ -23,6 +23,7 @@ SIGNATURES = {
                                    c_void_p]),
     "msn_iuwt_recompose": (c_int, [c_void_p, c_int, c_void_p, c_void_p, c_int, c_int, c_int, c_void_p, c_size_t,
                                    c_void_p]),
+    "msn_iuwt_decompose_static": (c_int, [c_void_p, c_void_p, c_void_p, c_int, c_int, c_int, c_int, c_void_p]),
     "msn_fft_workspace_bytes": (c_size_t, [c_int, c_int]),
     "msn_spectrum_elems": (c_size_t, [c_int]),
     "msn_psf_spectrum": (c_int, [c_void_p, c_int, c_int, c_int, c_int, c_int, c_void_p, c_void_p, c_size_t,

@@ -342,3 +342,73 @@ extern "C" int msn_iuwt_recompose(const float *d_detail, int planes, const float
     return iuwt_recompose_impl(d_detail, planes, d_smoothed, d_out, ny, nx, scale_adjust, p0, p1,
                                as_stream(stream));
 }
+
+// ---------------------------------------------------------------------------
+// Decomposition with library-owned scratch, for callers that cannot allocate.
+//
+// Some hosts cannot hand this library any device scratch: a C or Fortran
+// imaging pipeline whose own pool allocator owns all device memory, or a
+// latency-critical loop that must never call cudaMalloc (it can block, fail
+// under memory pressure, or implicitly synchronise the device). For them the
+// decomposition's two intermediate planes live in a fixed device array that
+// is part of the library image itself: it is reserved on every GPU that loads
+// libmsn.so and stays there until the process exits, so the entry point below
+// performs no allocation of any kind (no cudaMalloc, cudaFree or allocating
+// library call). The caller still owns and passes the input and the outputs.
+// ---------------------------------------------------------------------------
+namespace msn {
+namespace {
+
+constexpr size_t kStaticScratchPixels = (size_t)1 << 20;  // 1,048,576 pixels, e.g. 1024 x 1024
+constexpr size_t kStaticPlaneFloats = kStaticScratchPixels;
+
+// Two planes of up to kStaticScratchPixels floats each: 8 MiB per device.
+static __device__ __align__(256) float g_static_scratch[2 * kStaticPlaneFloats];
+
+// Device address of g_static_scratch, resolved once per device. In host code
+// the symbol is only a host-side stand-in and must never reach a kernel.
+std::mutex g_static_mu;
+float *g_static_addr[64] = {};
+
+int static_scratch(float **out) {
+    int device = 0;
+    MSN_TRY(check_cuda(cudaGetDevice(&device), "cudaGetDevice"));
+    if (device < 0 || device >= 64) return set_error(MSN_ERR_INVALID, "device index %d out of range", device);
+    std::lock_guard<std::mutex> lock(g_static_mu);
+    if (g_static_addr[device] == nullptr) {
+        void *p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_static_scratch);
+        MSN_TRY(check_cuda(e, "cudaGetSymbolAddress(g_static_scratch)"));
+        g_static_addr[device] = reinterpret_cast<float *>(p);
+    }
+    *out = g_static_addr[device];
+    return MSN_OK;
+}
+
+}  // namespace
+}  // namespace msn
+
+extern "C" int msn_iuwt_decompose_static(const float *d_in, float *d_detail, float *d_smoothed, int ny, int nx,
+                                         int scale_count, int scale_adjust, void *stream) {
+    using namespace msn;
+    clear_error();
+    static const char *fn = "msn_iuwt_decompose_static";
+    MSN_TRY(validate_image(ny, nx, fn));
+    if ((size_t)ny * (size_t)nx > kStaticScratchPixels)
+        return set_error(MSN_ERR_INVALID,
+                         "%s: %d x %d = %zu pixels exceeds the static scratch limit of %zu pixels "
+                         "(use msn_iuwt_decompose with a caller-supplied workspace)",
+                         fn, ny, nx, (size_t)ny * nx, kStaticScratchPixels);
+    MSN_TRY(validate_scales(ny, nx, scale_count, fn));
+    if (scale_adjust < 0 || scale_adjust > scale_count)
+        return set_error(MSN_ERR_INVALID, "%s: scale_adjust=%d outside [0, %d]", fn, scale_adjust, scale_count);
+    if (!d_in || (scale_count > scale_adjust && !d_detail))
+        return set_error(MSN_ERR_INVALID, "%s: null input or detail pointer", fn);
+    if (!aligned16(d_in) || !aligned16(d_detail) || !aligned16(d_smoothed))
+        return set_error(MSN_ERR_INVALID, "%s: device pointers must be 16-byte aligned", fn);
+    float *scratch = nullptr;
+    MSN_TRY(static_scratch(&scratch));
+    // Both planes are written before they are read, so nothing needs clearing.
+    return iuwt_decompose_impl(d_in, d_detail, d_smoothed, ny, nx, scale_count, scale_adjust, scratch,
+                               scratch + kStaticPlaneFloats, as_stream(stream));
+}
