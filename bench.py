@@ -1,17 +1,23 @@
-"""Benchmark of the PyMORESANE hot path on GB300.
+"""Benchmark of the PyMORESANE deconvolution hot path on GB300.
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload iuwt]
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload deconv|iuwt]
 
-Workload ``iuwt`` (default): the IUWT drop-in microbenchmark -- a 4096 x 4096
-float32 image (N(0,1) noise + 500 seeded deltas of amplitude U(5,50)),
-decomposed with scale_count=8, scale_adjust=0, store_smoothed=True, then
-recomposed from the detail stack and the smoothed plane. One step = one
-decomposition + one recomposition. Metric: algorithmic GB/s, with the
-algorithmic bytes of one step = 4 N^2 (1 + 8 + 1) for the decomposition plus
-4 N^2 (8 + 1 + 1) for the recomposition = 1.342 GB.
+Workload ``deconv`` (default) -- full single-image MORESANE at 2048 x 2048
+(float32 dirty image, 4096 x 4096 PSF from 20000 seeded uv points, 1000 point
+sources log-uniform in [1e-3, 1], 50 Gaussians with sigma 2-20 px, noise
+sigma 1e-4; scale_count=7, sigma_level=4, loop_gain=0.2, tolerance=0.75,
+accuracy=1e-6, major_loop_miter=100, minor_loop_miter=30, linear
+convolution). One step = one complete deconvolution (PSF spectra, major and
+minor loops, residual) of an image resident in HBM. Metric: deconvolutions
+per second, with the p50 / p99 latency of the steps; the same line carries the
+IUWT microbenchmark (4096^2, 8 scales) in GB/s.
 
-Rank 0 prints one JSON line. Multi-GPU runs are independent replicas (each
-rank transforms its own image; no collective on the data path).
+Workload ``iuwt`` -- 4096 x 4096 image (N(0,1) + 500 deltas U(5,50)),
+decomposition with scale_count=8, store_smoothed, then recomposition; metric:
+algorithmic GB/s, 4 N^2 (1 + 8 + 1) + 4 N^2 (8 + 1 + 1) bytes per step.
+
+Rank 0 prints one JSON line. With N > 1 GPUs (torchrun) every rank processes
+its own image (replicas, no collective on the data path; weak scaling).
 """
 import argparse
 import json
@@ -29,6 +35,13 @@ sys.path.insert(0, ROOT)
 
 PEAKS_PATH = os.path.join(ROOT, "MEASURED_PEAKS.json")
 FALLBACK_HBM_GBS = 6800.0
+DECONV_KW = dict(scale_count=7, sigma_level=4, loop_gain=0.2, tolerance=0.75, accuracy=1e-6, major_loop_miter=100,
+                 minor_loop_miter=30, conv_mode="linear")
+# Trajectory of the seed-0 2048^2 workload (major, minor iterations) as run by this
+# implementation on a GB300; used only to scale the CPU samples of the reference
+# arm, which cannot run a whole deconvolution in minutes.
+DECONV_TRAJECTORY = (90, 1419)
+IUWT_N, IUWT_S = 4096, 8
 
 
 def load_peaks():
@@ -97,55 +110,43 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-# ---------------------------------------------------------------------------
-# Workload: IUWT 4096^2, 8 scales
-# ---------------------------------------------------------------------------
+def gpu_uuid():
+    import torch
+    u = getattr(torch.cuda.get_device_properties(torch.cuda.current_device()), "uuid", None)
+    return ("GPU-" + str(u)) if u else None
 
-IUWT_N, IUWT_S = 4096, 8
 
+def percentile(vals, q):
+    return float(np.percentile(np.asarray(vals), q)) if vals else None
+
+
+def launches(reset=False):
+    from pymoresane_gb300 import _native
+    return int(_native.query("msn_launch_count", 1 if reset else 0))
+
+
+# ---------------------------------------------------------------------------
+# IUWT microbenchmark (4096^2, 8 scales)
+# ---------------------------------------------------------------------------
 
 def iuwt_algorithmic_bytes(n, s):
-    dec = 4 * n * n * (1 + s + 1)
-    rec = 4 * n * n * (s + 1 + 1)
-    return dec + rec
+    return 4 * n * n * (1 + s + 1) + 4 * n * n * (s + 1 + 1)
 
 
 def iuwt_kernel_bytes(n, s):
-    # Compulsory bytes of every atrous_band launch in one step: per scale the
+    # Compulsory bytes of the 3 s atrous_band launches of one step: per scale the
     # decomposition's smoothing (read 1 plane, write 1), its detail pass (read 2,
-    # write 1) and the recomposition's smoothing+add (read 2, write 1).
+    # write 1) and the recomposition's smoothing + add (read 2, write 1).
     return 4 * n * n * s * (2 + 3 + 3)
 
 
-def cpu_baseline_iuwt(kind, workers):
-    """Time the oracle port of the reference on a bounded sample (2048^2, 8 scales)."""
-    from oracle import iuwt as O
-    n = 2048
-    x = np.random.default_rng(5).standard_normal((n, n)).astype(np.float32)
-    t0 = time.perf_counter()
-    if workers == 1:
-        d, c = O.decompose(x, IUWT_S, 0, store_smoothed=True, arith="f64")
-        O.recompose(d, 0, smoothed_array=c, arith="f64")
-        sample = "2048^2, 8 scales, FP64 'ser' restatement (pymoresane/iuwt.py:66-191), 1 decomposition + 1 recomposition"
-    else:
-        d, c = O.decompose_strips(x, IUWT_S, 0, store_smoothed=True, workers=workers)
-        O.recompose_strips(d, 0, smoothed_array=c, workers=workers)
-        sample = (f"2048^2, 8 scales, FP32 strip-parallel 'mp' restatement (pymoresane/iuwt.py:193-382) on "
-                  f"{workers} threads, 1 decomposition + 1 recomposition")
-    dt = time.perf_counter() - t0
-    return iuwt_algorithmic_bytes(n, IUWT_S) / dt / 1e9, sample
-
-
-def run_iuwt(args, rank, world, dist):
+def measure_iuwt(steps, warmup, seed=0):
     import torch
 
     from pymoresane_gb300 import device as dev
-    from pymoresane_gb300 import iuwt as G
     from pymoresane_gb300 import synthetic
-
     n, s = IUWT_N, IUWT_S
-    x_host = synthetic.iuwt_image(n, 500, seed=rank)
-    x = torch.from_numpy(x_host).cuda()
+    x = torch.from_numpy(synthetic.iuwt_image(n, 500, seed=seed)).cuda()
     w = torch.empty((s, n, n), dtype=torch.float32, device="cuda")
     c = torch.empty((n, n), dtype=torch.float32, device="cuda")
     rec = torch.empty((n, n), dtype=torch.float32, device="cuda")
@@ -155,14 +156,119 @@ def run_iuwt(args, rank, world, dist):
         dev.iuwt_decompose(x, s, 0, store_smoothed=True, out=w, smoothed_out=c, work=work)
         dev.iuwt_recompose(w, 0, smoothed=c, out=rec, work=work)
 
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         step()
     torch.cuda.synchronize()
     err = torch.max(torch.abs(rec - x)).item()
-    assert err <= 1e-5 * torch.max(torch.abs(x)).item(), f"reconstruction error {err}"
+    assert err <= 1e-5 * torch.max(torch.abs(x)).item(), f"IUWT reconstruction error {err}"
+    stream = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    launches(reset=True)
+    e0.record(stream)
+    for _ in range(steps):
+        step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    nl = launches() / steps
+    return {"ms_per_step": ms, "gbs": iuwt_algorithmic_bytes(n, s) / (ms * 1e-3) / 1e9,
+            "kernel_gbs": iuwt_kernel_bytes(n, s) / (ms * 1e-3) / 1e9, "launches_per_step": nl,
+            "x_host": None, "n": n, "s": s}
 
-    sampler = ClockSampler(getattr(torch.cuda.get_device_properties(0), "uuid", None) and
-                           "GPU-" + str(torch.cuda.get_device_properties(0).uuid)) if rank == 0 else None
+
+def iuwt_e2e(steps, seed=0):
+    import torch
+
+    from pymoresane_gb300 import iuwt as G
+    from pymoresane_gb300 import synthetic
+    n, s = IUWT_N, IUWT_S
+    x_host = synthetic.iuwt_image(n, 500, seed=seed)
+    x_pin = torch.from_numpy(x_host).pin_memory()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        wd, cd = G.iuwt_decomposition(x_pin, s, 0, mode="gpu", store_smoothed=True)
+        rh = G.iuwt_recomposition(wd, 0, mode="gpu", smoothed_array=cd)
+    torch.cuda.synchronize()
+    dt = (time.perf_counter() - t0) / steps
+    assert np.max(np.abs(rh - x_host)) <= 1e-5 * np.max(np.abs(x_host))
+    return dt
+
+
+def cpu_iuwt(workers):
+    """Oracle port of the reference IUWT on a bounded 2048^2 sample (GB/s)."""
+    from oracle import iuwt as O
+    n = 2048
+    x = np.random.default_rng(5).standard_normal((n, n)).astype(np.float32)
+    t0 = time.perf_counter()
+    if workers == 1:
+        d, c = O.decompose(x, IUWT_S, 0, store_smoothed=True, arith="f64")
+        O.recompose(d, 0, smoothed_array=c, arith="f64")
+        sample = ("2048^2, 8 scales: one decomposition + recomposition of the FP64 'ser' restatement "
+                  "(pymoresane/iuwt.py:66-191), 1 thread")
+    else:
+        d, c = O.decompose_strips(x, IUWT_S, 0, store_smoothed=True, workers=workers)
+        O.recompose_strips(d, 0, smoothed_array=c, workers=workers)
+        sample = (f"2048^2, 8 scales: one decomposition + recomposition of the FP32 strip-parallel 'mp' "
+                  f"restatement (pymoresane/iuwt.py:193-382) on {workers} threads")
+    dt = time.perf_counter() - t0
+    return iuwt_algorithmic_bytes(n, IUWT_S) / dt / 1e9, sample
+
+
+# ---------------------------------------------------------------------------
+# Deconvolution workload (2048^2 MORESANE)
+# ---------------------------------------------------------------------------
+
+def deconv_problem(seed):
+    from pymoresane_gb300 import synthetic
+    dirty, psf, _ = synthetic.make_problem(synthetic.config2(seed))
+    return dirty, psf
+
+
+def cpu_deconv(dirty, psf, decom, workers, trajectory):
+    """Oracle port of the reference MORESANE timed on a bounded sample, scaled to one deconvolution.
+
+    The sample is the set-up (PSF spectra and energies) plus the first major
+    iteration with its first two minor iterations; the per-major and
+    per-minor times are scaled by the trajectory (major, minor) of a full run.
+    """
+    from oracle.moresane import MoresaneOracle
+    o = MoresaneOracle(dirty, psf, decom=decom, workers=workers)
+    t0 = time.perf_counter()
+    o.moresane(**dict(DECONV_KW, major_loop_miter=1, minor_loop_miter=2))
+    wall = time.perf_counter() - t0
+    t = o.timings
+    per_major = t["major"] / max(1, t["n_major"])
+    per_minor = t["minor"] / max(1, t["n_minor"])
+    n_major, n_minor = trajectory
+    seconds = t["setup"] + n_major * per_major + n_minor * per_minor
+    sample = (f"2048^2 config: set-up + 1 major + {t['n_minor']} minor iterations of the oracle port "
+              f"({'FP64 ser' if decom == 'ser' else 'FP32 mp'} IUWT, numpy FFT, scipy labelling) in {wall:.1f} s, "
+              f"scaled to a full deconvolution of {n_major} major / {n_minor} minor iterations "
+              f"(per major {per_major:.2f} s, per minor {per_minor:.2f} s)")
+    return 1.0 / seconds, sample
+
+
+def run_deconv(args, rank, world, dist):
+    import torch
+
+    from pymoresane_gb300.main import DataImage, Deconvolver
+    dirty_h, psf_h = deconv_problem(rank)
+    dirty = torch.from_numpy(dirty_h).cuda()
+    psf = torch.from_numpy(psf_h).cuda()
+
+    def step():
+        eng = Deconvolver(psf)
+        model, residual, major = eng.moresane(dirty, **DECONV_KW)
+        return eng, model, residual
+
+    eng = None
+    for _ in range(args.warmup):
+        eng, model, residual = step()
+    torch.cuda.synchronize()
+    traj = (len(eng.log), sum(r.get("minor", 0) for r in eng.log))
+
+    sampler = ClockSampler(gpu_uuid()) if rank == 0 else None
     if sampler:
         sampler.start()
         time.sleep(0.3)
@@ -170,50 +276,87 @@ def run_iuwt(args, rank, world, dist):
         dist.barrier()
     torch.cuda.synchronize()
     stream = torch.cuda.current_stream()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
+    lat = []
+    launches(reset=True)
+    t_start = torch.cuda.Event(enable_timing=True)
+    t_start.record(stream)
+    prev = t_start
     for _ in range(args.steps):
         step()
-    e1.record(stream)
+        ev = torch.cuda.Event(enable_timing=True)
+        ev.record(stream)
+        ev.synchronize()
+        lat.append(prev.elapsed_time(ev))
+        prev = ev
     torch.cuda.synchronize()
+    n_launch = launches()
     if dist:
         dist.barrier()
-    ms = e0.elapsed_time(e1)
-    # extend the sampled window with a loop of the same work so nvidia-smi sees load
-    t_end = time.perf_counter() + 1.0
-    while time.perf_counter() < t_end:
-        step()
-        torch.cuda.synchronize()
+    total_ms = t_start.elapsed_time(prev)
     clocks = sampler.stop() if sampler else None
 
-    # end-to-end through the public API with host buffers (pinned input)
-    x_pin = torch.from_numpy(x_host).pin_memory()
-    e2e_steps = max(1, min(args.steps, 5))
+    # end to end through the public host-array API
+    e2e_steps = max(1, min(args.steps, 3))
     torch.cuda.synchronize()
-    if dist:
-        dist.barrier()
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
-        wd, cd = G.iuwt_decomposition(x_pin, s, 0, mode="gpu", store_smoothed=True)
-        rh = G.iuwt_recomposition(wd, 0, mode="gpu", smoothed_array=cd)
-    torch.cuda.synchronize()
+        img = DataImage(dirty_h, psf_h, None, 1.0, 1.0)
+        img.moresane(**DECONV_KW)
+        _ = float(img.model.sum())
     e2e_s = (time.perf_counter() - t0) / e2e_steps
-    assert np.max(np.abs(rh - x_host)) <= 1e-5 * np.max(np.abs(x_host))
 
-    t = torch.tensor([ms, e2e_s], dtype=torch.float64, device="cuda")
+    t = torch.tensor([total_ms, e2e_s], dtype=torch.float64, device="cuda")
     if dist:
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    ms, e2e_s = t.tolist()
-    return {"ms": ms, "e2e_s": e2e_s, "clocks": clocks, "n": n, "s": s, "e2e_steps": e2e_steps}
+    total_ms, e2e_s = t.tolist()
+    return {"ms": total_ms, "lat": lat, "e2e_s": e2e_s, "clocks": clocks, "traj": traj, "launches": n_launch,
+            "dirty": dirty_h, "psf": psf_h, "model_sum": float(img.model.sum()), "e2e_steps": e2e_steps}
+
+
+def conv_roofline(n=2048, m=4096, reps=50):
+    """Average duration of the fused linear convolution (the minor loop's dominant step) at 2048^2 / 4096^2.
+
+    Algorithmic bytes per convolution: read x (4 n^2) + read the
+    PSF spectrum (8 m (m/2 + 1)) + write the result (4 n^2).
+    """
+    import torch
+
+    from pymoresane_gb300 import device as dev
+    from pymoresane_gb300.synthetic import make_psf
+    psf = make_psf(m, 2000, np.random.default_rng(1))
+    spec = dev.psf_spectrum(psf)
+    x = torch.randn((n, n), device="cuda")
+    out = torch.empty_like(x)
+    work = dev.fft_workspace(n, m, x.device)
+    for _ in range(3):
+        dev.fft_convolve(x, spec, True, out=out, work=work)
+    stream = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(reps):
+        dev.fft_convolve(x, spec, True, out=out, work=work)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    us = e0.elapsed_time(e1) * 1e3 / reps
+    alg = 4 * n * n + 8 * m * (m // 2 + 1) + 4 * n * n
+    return us, alg
+
+
+def read_traffic(name):
+    try:
+        with open(os.path.join(ROOT, "profiles", name)) as fh:
+            return json.load(fh)
+    except Exception:
+        return None
 
 
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
-    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="iuwt", choices=["iuwt"])
+    ap.add_argument("--workload", default="deconv", choices=["deconv", "iuwt", "conv"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
@@ -221,26 +364,35 @@ def main():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     hbm_peak, peak_kind = load_peaks()
-    metric = "IUWT algorithmic HBM GB/s (4096^2, scale_count=8, decomposition+recomposition)"
+    if args.workload == "deconv":
+        metric = "2048^2 deconvolutions/s (MORESANE, 4096^2 PSF, scale_count=7, 1 GB300)"
+        unit = "deconv/s"
+    else:
+        metric = "IUWT algorithmic HBM GB/s (4096^2, scale_count=8, decomposition+recomposition)"
+        unit = "GB/s"
 
     if args.impl == "reference":
         if rank != 0:
             return
         workers = os.cpu_count() or 1
-        vals = []
+        vals, sample = [], None
+        if args.workload == "deconv":
+            dirty, psf = deconv_problem(0)
         for i in range(args.warmup + args.steps):
-            v, sample = cpu_baseline_iuwt("reference", workers)
+            if args.workload == "deconv":
+                v, sample = cpu_deconv(dirty, psf, "mp", workers, DECONV_TRAJECTORY)
+            else:
+                v, sample = cpu_iuwt(workers)
             if i >= args.warmup:
                 vals.append(v)
         value = statistics.mean(vals)
         print(json.dumps({
-            "impl": "reference", "metric": metric, "value": round(value, 4), "unit": "GB/s", "n_gpus": args.gpus,
+            "impl": "reference", "metric": metric, "value": value, "unit": unit, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": "iuwt 4096^2 S=8 (sampled at 2048^2 on the host)", "parallelism": "host threads"},
-            "cpu_baseline": {"value": round(value, 4), "unit": "GB/s", "cores": workers, "kind": "port",
-                             "sample": sample},
-            "e2e": {"value": round(value, 4), "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "config": {"workload": args.workload, "parallelism": f"host, {workers} threads"},
+            "cpu_baseline": {"value": value, "unit": unit, "cores": workers, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         }))
         return
 
@@ -254,52 +406,90 @@ def main():
     else:
         torch.cuda.set_device(0)
 
-    res = run_iuwt(args, rank, world, dist)
-    n, s = res["n"], res["s"]
-    ms_per_step = res["ms"] / args.steps
-    alg = iuwt_algorithmic_bytes(n, s)
-    value = world * alg / (ms_per_step * 1e-3) / 1e9
-    kern_bytes = iuwt_kernel_bytes(n, s)
-    launches_per_step = 3 * s
-    achieved = kern_bytes / (ms_per_step * 1e-3) / 1e9
-    e2e_value = world * alg / res["e2e_s"] / 1e9
-    h2d = 4 * n * n + 4 * n * n * (s + 1)
-    d2h = 4 * n * n * (s + 1) + 4 * n * n
+    if args.workload == "conv":
+        # Fused linear FFT convolution microbenchmark: 2048^2 image, 4096^2 PSF spectrum.
+        us, alg = conv_roofline(reps=max(args.steps, 1))
+        if rank == 0:
+            print(json.dumps({"metric": "fused FFT convolution algorithmic GB/s (2048^2 image, 4096^2 PSF, linear)",
+                              "value": alg / (us * 1e-6) / 1e9, "unit": "GB/s", "n_gpus": world, "steps": args.steps,
+                              "warmup": args.warmup, "us_per_conv": us, "algorithmic_bytes": alg,
+                              "frac_of_hbm": alg / (us * 1e-6) / 1e9 / hbm_peak}))
+        return
 
+    if args.workload == "iuwt":
+        sampler = ClockSampler(gpu_uuid()) if rank == 0 else None
+        if sampler:
+            sampler.start()
+            time.sleep(0.3)
+        if dist:
+            dist.barrier()
+        r = measure_iuwt(args.steps, args.warmup, seed=rank)
+        t = torch.tensor([r["ms_per_step"]], dtype=torch.float64, device="cuda")
+        if dist:
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+        clocks = sampler.stop() if sampler else None
+        e2e_s = iuwt_e2e(max(1, min(args.steps, 5)), seed=rank)
+        n, s = IUWT_N, IUWT_S
+        alg = iuwt_algorithmic_bytes(n, s)
+        if rank == 0:
+            cpu = None
+            if not args.no_cpu_baseline:
+                v, sample = cpu_iuwt(1)
+                cpu = {"value": v, "unit": "GB/s", "cores": 1, "kind": "port", "sample": sample}
+            print(json.dumps({
+                "metric": metric, "value": world * alg / (ms * 1e-3) / 1e9, "unit": unit, "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                "config": {"workload": "iuwt_4096x4096_S8_store_smoothed (BASELINE config 1)",
+                           "l2": "working set 0.7 GB per step > 129 MB L2 (no flush needed)",
+                           "parallelism": f"replicas x{world}"},
+                "roofline": {"bound": "hbm", "kernel": "atrous_band", "achieved": r["kernel_gbs"], "peak": hbm_peak,
+                             "peak_kind": peak_kind, "unit": "GB/s", "frac": r["kernel_gbs"] / hbm_peak,
+                             "traffic": (read_traffic("iuwt_traffic.json") or {}).get("bytes_per_launch")},
+                "e2e": {"value": world * alg / e2e_s / 1e9, "unit": "GB/s", "h2d_bytes_per_step": 4 * n * n * (s + 2),
+                        "d2h_bytes_per_step": 4 * n * n * (s + 2)},
+                "gpu_launches": int(r["launches_per_step"] * args.steps), "clocks": clocks, "cpu_baseline": cpu,
+            }))
+        if dist:
+            dist.destroy_process_group()
+        return
+
+    res = run_deconv(args, rank, world, dist)
+    ms_per_step = res["ms"] / args.steps
+    value = world * args.steps / (res["ms"] * 1e-3)
+    iuwt = measure_iuwt(5, 3, seed=rank)
+    conv_us, conv_alg = conv_roofline()
+    conv_gbs = conv_alg / (conv_us * 1e-6) / 1e9
     if rank == 0:
         cpu = None
         if not args.no_cpu_baseline:
-            v, sample = cpu_baseline_iuwt("port", 1)
-            cpu = {"value": round(v, 4), "unit": "GB/s", "cores": 1, "kind": "port", "sample": sample}
-        traffic = None
-        try:
-            with open(os.path.join(ROOT, "profiles", "iuwt_traffic.json")) as fh:
-                traffic = json.load(fh).get("bytes_per_launch")
-        except Exception:
-            pass
-        line = {
-            "metric": metric, "value": round(value, 2), "unit": "GB/s", "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": round(ms_per_step, 4), "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": "iuwt_4096x4096_S8_store_smoothed (BASELINE config 1)", "n": n,
-                       "scale_count": s, "scale_adjust": 0, "step": "decomposition + recomposition",
-                       "l2": "working set 0.7 GB per step > 129 MB L2 (no flush needed)",
+            v, sample = cpu_deconv(res["dirty"], res["psf"], "ser", 1, res["traj"])
+            cpu = {"value": v, "unit": "deconv/s", "cores": 1, "kind": "port", "sample": sample}
+        n = 2048
+        m = 4096
+        print(json.dumps({
+            "metric": metric, "value": value, "unit": unit, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "moresane_2048x2048_psf4096_S7_linear (BASELINE config 2)",
+                       "trajectory_major_minor": list(res["traj"]),
+                       "l2": "working set > 0.6 GB per deconvolution > 129 MB L2 (no flush needed)",
                        "parallelism": f"replicas x{world}"},
-            "algorithmic_bytes_per_step": alg,
-            "step_frac_of_hbm": round(value / world / hbm_peak, 4),
-            "roofline": {"bound": "hbm", "kernel": "atrous_band (all epilogues)",
-                         "achieved": round(achieved, 1), "peak": hbm_peak, "peak_kind": peak_kind,
-                         "unit": "GB/s", "frac": round(achieved / hbm_peak, 4), "traffic": traffic,
-                         "bytes_per_launch_avg": kern_bytes // launches_per_step,
-                         "avg_launch_us": round(ms_per_step * 1e3 / launches_per_step, 2)},
-            "e2e": {"value": round(e2e_value, 2), "unit": "GB/s", "h2d_bytes_per_step": h2d,
-                    "d2h_bytes_per_step": d2h, "steps": res["e2e_steps"],
-                    "api": "pymoresane_gb300.iuwt.iuwt_decomposition + iuwt_recomposition (numpy/pinned host)"},
-            "gpu_launches": launches_per_step * args.steps,
-            "clocks": res["clocks"],
-            "cpu_baseline": cpu,
-        }
-        print(json.dumps(line))
+            "latency_ms": {"p50": percentile(res["lat"], 50), "p99": percentile(res["lat"], 99),
+                           "mode": "plain (one image at a time)"},
+            "iuwt_gbs": iuwt["gbs"], "iuwt_frac_of_hbm": iuwt["gbs"] / hbm_peak,
+            "roofline": {"bound": "hbm", "kernel": "fft_convolve (rfft_rows + conv_cols + irfft_rows), linear "
+                                                  "2048^2 image / 4096^2 PSF",
+                         "achieved": conv_gbs, "peak": hbm_peak, "peak_kind": peak_kind, "unit": "GB/s",
+                         "frac": conv_gbs / hbm_peak, "avg_launch_us": conv_us,
+                         "algorithmic_bytes_per_launch": conv_alg,
+                         "traffic": (read_traffic("conv_traffic.json") or {}).get("bytes_per_launch")},
+            "e2e": {"value": world / res["e2e_s"], "unit": unit, "h2d_bytes_per_step": 4 * n * n + 4 * m * m,
+                    "d2h_bytes_per_step": 8 * n * n, "steps": res["e2e_steps"],
+                    "api": "pymoresane_gb300.main.DataImage(dirty, psf).moresane(...) with host numpy arrays"},
+            "gpu_launches": res["launches"], "clocks": res["clocks"], "cpu_baseline": cpu,
+        }))
     if dist:
         dist.destroy_process_group()
 

@@ -42,6 +42,10 @@ const char *msn_last_error(void);
 /* ABI version of this library (major * 10000 + minor * 100 + patch). */
 int msn_version(void);
 
+/* Number of kernels this library has launched in the process (all threads);
+ * reset != 0 returns the count and sets it back to zero. Diagnostics only. */
+unsigned long long msn_launch_count(int reset);
+
 /* ---------------------------------------------------------------------------
  * IUWT (a trous, B3 spline [1,4,6,4,1]/16, dilation 2^s, mirror borders)
  * ------------------------------------------------------------------------- */
@@ -60,6 +64,14 @@ size_t msn_iuwt_workspace_bytes(int ny, int nx);
 int msn_iuwt_decompose(const float *d_in, float *d_detail, float *d_smoothed, int ny, int nx,
                        int scale_count, int scale_adjust, void *d_work, size_t work_bytes,
                        void *stream);
+
+/* Decomposition with the source mask applied in the detail pass:
+ * d_detail[s] = d_mask[s] * w_s (float32 product), d_mask and d_detail
+ * [scale_count - scale_adjust][ny][nx]. Replaces the minor-loop sequence
+ * iuwt_decomposition(...) followed by extracted_sources_mask * Ap
+ * (pymoresane/main.py:381-383,400-402,414-416) in one set of passes. */
+int msn_iuwt_decompose_masked(const float *d_in, const float *d_mask, float *d_detail, int ny, int nx,
+                              int scale_count, int scale_adjust, void *d_work, size_t work_bytes, void *stream);
 
 /* Replaces iuwt_recomposition(in1, scale_adjust, mode='gpu',
  * smoothed_array=...) -- pymoresane/iuwt.py:43 -> gpu_iuwt_recomposition

@@ -13,6 +13,8 @@ Every major iteration appends a record to ``self.log`` (min_scale,
 max_scale, scale_adjust, minor iterations, final SNR, residual std) so that
 trajectories can be compared decision by decision.
 """
+import time
+
 import numpy as np
 
 from . import convolution as C
@@ -46,7 +48,14 @@ def suppression_array(scale_count, subregion, edge_suppression, edge_offset):
 
 
 class MoresaneOracle:
-    def __init__(self, dirty, psf, mask=None, precision="ref"):
+    """``decom='mp'`` swaps the 'ser' IUWT for the strip-parallel FP32 'mp'
+    restatement on ``workers`` threads (the reference's mode='mp',
+    pymoresane/iuwt.py:193-382). ``self.timings`` accumulates wall time of the
+    set-up, of the per-major-iteration work and of the minor iterations."""
+
+    def __init__(self, dirty, psf, mask=None, precision="ref", decom="ser", workers=1):
+        self.decom, self.workers = decom, workers
+        self.timings = {"setup": 0.0, "major": 0.0, "minor": 0.0, "n_major": 0, "n_minor": 0}
         self.f64 = precision == "f64"
         dt = np.float64 if self.f64 else np.float32
         self.dirty_data = np.asarray(dirty).astype(dt)
@@ -68,10 +77,23 @@ class MoresaneOracle:
             subregion = n
         if scale_count is None or scale_count > (np.log2(n) - 1):
             scale_count = int(np.log2(n) - 1)
+        t_setup = time.perf_counter()
+        if self.decom == "mp":
+            def dec_fn(x, s, adj):
+                return I.decompose_strips(x, s, adj, workers=self.workers)
+
+            def rec_fn(w, adj):
+                return I.recompose_strips(w, adj, workers=self.workers)
+        else:
+            def dec_fn(x, s, adj):
+                return I.decompose(x, s, adj, arith="f64")
+
+            def rec_fn(w, adj):
+                return I.recompose(w, adj, arith="f64")
         sub_fft, data_fft, psf_sub, sub_sl = C.psf_spectra(self.psf_data, self.dirty_data.shape, subregion, conv_mode)
         dirty_sub = self.dirty_data[sub_sl]
 
-        psf_dec = I.decompose(psf_sub, scale_count, 0, arith="f64")
+        psf_dec = dec_fn(psf_sub, scale_count, 0)
         energies = np.empty([psf_dec.shape[0], 1, 1], dtype=np.float32)
         for i in range(energies.shape[0]):
             energies[i] = np.sqrt(np.sum(np.square(psf_dec[i])))
@@ -84,15 +106,17 @@ class MoresaneOracle:
         supp = suppression_array(scale_count, subregion, edge_suppression, edge_offset)
         residual = None
         x = None
+        self.timings["setup"] += time.perf_counter() - t_setup
+        t_major = time.perf_counter()
         while (major < major_loop_miter and max_coeff > 0 and std_ratio > accuracy
                and np.max(dirty_sub) > flux_threshold):
             rec = {"major": major}
             while min_scale < scale_count:
                 if min_scale == 0:
-                    dec = I.decompose(dirty_sub, scale_count, 0, arith="f64")
+                    dec = dec_fn(dirty_sub, scale_count, 0)
                     thresholds = T.estimate_threshold(dec, edge_excl, int_excl)
                     if self.mask is not None:
-                        dec = I.decompose(dirty_sub * self.mask[sub_sl], scale_count, 0, arith="f64")
+                        dec = dec_fn(dirty_sub * self.mask[sub_sl], scale_count, 0)
                     dec_thr = T.apply_threshold(dec, thresholds, sigma_level=sigma_level)
                     if supp is not None:
                         dec_thr *= supp
@@ -111,12 +135,12 @@ class MoresaneOracle:
                         break
                 extracted, ext_mask = T.source_extraction(dec_thr[scale_adjust:max_scale], tolerance, neg_comp,
                                                           semantics="cpu")
-                recomposed = I.recompose(extracted, scale_adjust, arith="f64")
+                recomposed = rec_fn(extracted, scale_adjust)
 
                 def apply_a(v):
                     a = _conv(v, sub_fft, conv_mode, self.f64)
-                    a = I.decompose(a, max_scale, scale_adjust, arith="f64")
-                    return I.recompose(ext_mask * a, scale_adjust, arith="f64")
+                    a = dec_fn(a, max_scale, scale_adjust)
+                    return rec_fn(ext_mask * a, scale_adjust)
 
                 x = np.zeros_like(recomposed)
                 r = recomposed.copy()
@@ -124,6 +148,7 @@ class MoresaneOracle:
                 minor = 0
                 snr_last = snr_current = 0
                 while minor < minor_loop_miter:
+                    t_minor = time.perf_counter()
                     ap = apply_a(p)
                     alpha = np.dot(r.reshape(1, -1), r.reshape(-1, 1))[0, 0] / np.dot(p.reshape(1, -1),
                                                                                      ap.reshape(-1, 1))[0, 0]
@@ -137,10 +162,14 @@ class MoresaneOracle:
                             / np.dot(r.reshape(1, -1), r.reshape(-1, 1))[0, 0])
                     p = rn + beta * p
                     ms = _conv(xn, sub_fft, conv_mode, self.f64)
-                    ms = ext_mask * I.decompose(ms, max_scale, scale_adjust, arith="f64")
+                    ms = ext_mask * dec_fn(ms, max_scale, scale_adjust)
                     snr_last = snr_current
                     snr_current = T.snr_ratio(extracted, ms)
                     minor += 1
+                    dt = time.perf_counter() - t_minor
+                    self.timings["minor"] += dt
+                    self.timings["n_minor"] += 1
+                    t_major += dt
                     if minor == 1 and snr_current > 40:
                         min_scale += 1
                         break
@@ -178,6 +207,10 @@ class MoresaneOracle:
                 dirty_sub = residual[sub_sl]
                 major += 1
                 self.log.append(rec)
+                now = time.perf_counter()
+                self.timings["major"] += now - t_major
+                self.timings["n_major"] += 1
+                t_major = now
             if major == 0:
                 self.complete = True
                 break

@@ -18,9 +18,12 @@ c_int, c_size_t, c_void_p, c_float, c_double = (ctypes.c_int, ctypes.c_size_t, c
 SIGNATURES = {
     "msn_last_error": (ctypes.c_char_p, []),
     "msn_version": (c_int, []),
+    "msn_launch_count": (ctypes.c_ulonglong, [c_int]),
     "msn_iuwt_workspace_bytes": (c_size_t, [c_int, c_int]),
     "msn_iuwt_decompose": (c_int, [c_void_p, c_void_p, c_void_p, c_int, c_int, c_int, c_int, c_void_p, c_size_t,
                                    c_void_p]),
+    "msn_iuwt_decompose_masked": (c_int, [c_void_p, c_void_p, c_void_p, c_int, c_int, c_int, c_int, c_void_p,
+                                          c_size_t, c_void_p]),
     "msn_iuwt_recompose": (c_int, [c_void_p, c_int, c_void_p, c_void_p, c_int, c_int, c_int, c_void_p, c_size_t,
                                    c_void_p]),
     "msn_iuwt_decompose_static": (c_int, [c_void_p, c_void_p, c_void_p, c_int, c_int, c_int, c_int, c_void_p]),

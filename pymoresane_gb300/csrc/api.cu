@@ -1,4 +1,5 @@
 // libmsn: error reporting and version query.
+#include <atomic>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
@@ -24,7 +25,15 @@ int check_cuda(cudaError_t e, const char *what) {
     return set_error(MSN_ERR_CUDA, "%s: %s (%s)", what, cudaGetErrorString(e), cudaGetErrorName(e));
 }
 
+static std::atomic<unsigned long long> g_launches{0};
+
+void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+
 }  // namespace msn
+
+extern "C" unsigned long long msn_launch_count(int reset) {
+    return reset ? msn::g_launches.exchange(0) : msn::g_launches.load();
+}
 
 extern "C" const char *msn_last_error(void) { return msn::g_last_error; }
 

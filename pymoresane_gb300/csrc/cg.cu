@@ -2,7 +2,8 @@
 // (pymoresane/main.py:365-503) for sm_103a.
 //
 // Every inner product, the step sizes alpha / beta and the residual
-// statistics are accumulated in float64. Reductions are deterministic: a
+// statistics are accumulated in float64 (four-element float32 partials, see
+// dot4). Reductions are deterministic: a
 // fixed grid writes one float64 partial per CTA and a single CTA sums the
 // partials in a fixed order, so results are bit-identical run to run and do
 // not depend on what else shares the GPU. The CG scalars live in a small
@@ -31,19 +32,34 @@ __device__ __forceinline__ double block_sum(double v) {
     return v;  // valid in thread 0
 }
 
+// Float64 accumulation at a low float64 instruction count (the FP64 rate of
+// GB300 is a small fraction of its FP32 rate): every thread forms the products
+// of four consecutive elements with a float32 fused multiply-add chain, then
+// adds that four-element partial to its float64 accumulator (one conversion
+// and one float64 add per four elements). The relative error of each
+// four-element partial is a few float32 ulps; all longer sums are float64.
+__device__ __forceinline__ float dot4(const float4 &a, const float4 &b) {
+    return __fmaf_rn(a.w, b.w, __fmaf_rn(a.z, b.z, __fmaf_rn(a.y, b.y, __fmul_rn(a.x, b.x))));
+}
+__device__ __forceinline__ float sqdiff4(const float4 &a, const float4 &b) {
+    const float x = __fsub_rn(a.x, b.x), y = __fsub_rn(a.y, b.y), z = __fsub_rn(a.z, b.z), w = __fsub_rn(a.w, b.w);
+    return __fmaf_rn(w, w, __fmaf_rn(z, z, __fmaf_rn(y, y, __fmul_rn(x, x))));
+}
+
 // partials[2*b + 0] = sum a*b, partials[2*b + 1] = sum c*d (or sum (a - c)^2 when DIFF).
+// n4 float4 groups (callers guarantee n % 4 == 0 and 16-byte alignment).
 template <bool DIFF>
 __global__ void __launch_bounds__(kRedThreads)
-dual_partials(const float *__restrict__ a, const float *__restrict__ b, const float *__restrict__ c,
-              const float *__restrict__ d, size_t n, double *__restrict__ partials) {
+dual_partials(const float4 *__restrict__ a, const float4 *__restrict__ b, const float4 *__restrict__ c,
+              const float4 *__restrict__ d, size_t n4, double *__restrict__ partials) {
     double s0 = 0.0, s1 = 0.0;
-    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-        s0 += (double)a[i] * (double)b[i];
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n4; i += (size_t)gridDim.x * blockDim.x) {
+        const float4 va = __ldg(a + i);
+        s0 += (double)dot4(va, __ldg(b + i));
         if (DIFF) {
-            const double t = (double)a[i] - (double)c[i];
-            s1 += t * t;
+            s1 += (double)sqdiff4(va, __ldg(c + i));
         } else if (c) {
-            s1 += (double)c[i] * (double)d[i];
+            s1 += (double)dot4(__ldg(c + i), __ldg(d + i));
         }
     }
     s0 = block_sum(s0);
@@ -74,16 +90,28 @@ __global__ void __launch_bounds__(1024) finalize_pairs(const double *__restrict_
     }
 }
 
+// The vector updates evaluate the reference's float32 expressions
+// (pymoresane/main.py:390,397,405,411 on float32 arrays in GPU mode) with
+// alpha and beta computed in float64 from the float64 inner products and then
+// rounded to float32: xn = x + a*p, p = (xn - x)/a, rn = r - a*Ap,
+// p = rn + b*p, each product and sum rounded separately (no contraction).
+
 // xn = x + alpha p with alpha = rr / pAp (main.py:386-390); counts xn < 0.
-__global__ void cg_alpha_x(const float *__restrict__ x, const float *__restrict__ p, double *__restrict__ scal,
-                           float *__restrict__ xn, size_t n, int *__restrict__ neg) {
+__global__ void cg_alpha_x(const float4 *__restrict__ x, const float4 *__restrict__ p, double *__restrict__ scal,
+                           float4 *__restrict__ xn, size_t n4, int *__restrict__ neg) {
     const double alpha = scal[S_RR] / scal[S_PAP];
     if (blockIdx.x == 0 && threadIdx.x == 0) scal[S_ALPHA] = alpha;
+    const float a = (float)alpha;
     int local = 0;
-    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-        const float v = (float)__dadd_rn((double)x[i], __dmul_rn(alpha, (double)p[i]));
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n4; i += (size_t)gridDim.x * blockDim.x) {
+        const float4 xv = __ldg(x + i), pv = __ldg(p + i);
+        float4 v;
+        v.x = __fadd_rn(xv.x, __fmul_rn(a, pv.x));
+        v.y = __fadd_rn(xv.y, __fmul_rn(a, pv.y));
+        v.z = __fadd_rn(xv.z, __fmul_rn(a, pv.z));
+        v.w = __fadd_rn(xv.w, __fmul_rn(a, pv.w));
         xn[i] = v;
-        local += v < 0.0f;
+        local += (v.x < 0.0f) + (v.y < 0.0f) + (v.z < 0.0f) + (v.w < 0.0f);
     }
     local = __reduce_add_sync(0xffffffffu, local);
     if ((threadIdx.x & 31) == 0 && local) atomicAdd(neg, local);
@@ -92,29 +120,30 @@ __global__ void cg_alpha_x(const float *__restrict__ x, const float *__restrict_
 // Positivity (main.py:394-397): xn[xn < 0] = 0; p = (xn - x) / alpha.
 __global__ void cg_positivity(const float *__restrict__ x, float *__restrict__ xn, float *__restrict__ p,
                               const double *__restrict__ scal, size_t n) {
-    const double alpha = scal[S_ALPHA];
+    const float a = (float)scal[S_ALPHA];
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
         float v = xn[i];
         if (v < 0.0f) v = 0.0f;
         xn[i] = v;
-        p[i] = (float)__ddiv_rn(__dsub_rn((double)v, (double)x[i]), alpha);
+        p[i] = __fdiv_rn(__fsub_rn(v, x[i]), a);
     }
 }
 
-// rn = r - alpha Ap with the per-CTA partial of rn . rn (main.py:405-408).
-// The vector updates use explicitly rounded float64 products and sums (no
-// contraction into fused multiply-adds) so that they reproduce a float64
-// evaluation of the reference expressions exactly before the final rounding
-// to float32.
+// rn = r - alpha Ap with the per-CTA float64 partial of rn . rn (main.py:405-408).
 __global__ void __launch_bounds__(kRedThreads)
-cg_residual(const float *__restrict__ r, const float *__restrict__ ap, const double *__restrict__ scal,
-            float *__restrict__ rn, size_t n, double *__restrict__ partials) {
-    const double alpha = scal[S_ALPHA];
+cg_residual(const float4 *__restrict__ r, const float4 *__restrict__ ap, const double *__restrict__ scal,
+            float4 *__restrict__ rn, size_t n4, double *__restrict__ partials) {
+    const float a = (float)scal[S_ALPHA];
     double s = 0.0;
-    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-        const float v = (float)__dsub_rn((double)r[i], __dmul_rn(alpha, (double)ap[i]));
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n4; i += (size_t)gridDim.x * blockDim.x) {
+        const float4 rv = __ldg(r + i), av = __ldg(ap + i);
+        float4 v;
+        v.x = __fsub_rn(rv.x, __fmul_rn(a, av.x));
+        v.y = __fsub_rn(rv.y, __fmul_rn(a, av.y));
+        v.z = __fsub_rn(rv.z, __fmul_rn(a, av.z));
+        v.w = __fsub_rn(rv.w, __fmul_rn(a, av.w));
         rn[i] = v;
-        s += (double)v * (double)v;
+        s += (double)dot4(v, v);
     }
     s = block_sum(s);
     if (threadIdx.x == 0) {
@@ -129,11 +158,18 @@ __global__ void cg_beta(double *__restrict__ scal) {
 }
 
 // p = rn + beta p (main.py:411).
-__global__ void cg_direction(const float *__restrict__ rn, float *__restrict__ p, const double *__restrict__ scal,
-                             size_t n) {
-    const double beta = scal[S_BETA];
-    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
-        p[i] = (float)__dadd_rn((double)rn[i], __dmul_rn(beta, (double)p[i]));
+__global__ void cg_direction(const float4 *__restrict__ rn, float4 *__restrict__ p, const double *__restrict__ scal,
+                             size_t n4) {
+    const float b = (float)scal[S_BETA];
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n4; i += (size_t)gridDim.x * blockDim.x) {
+        const float4 rv = __ldg(rn + i);
+        float4 pv = p[i];
+        pv.x = __fadd_rn(rv.x, __fmul_rn(b, pv.x));
+        pv.y = __fadd_rn(rv.y, __fmul_rn(b, pv.y));
+        pv.z = __fadd_rn(rv.z, __fmul_rn(b, pv.z));
+        pv.w = __fadd_rn(rv.w, __fmul_rn(b, pv.w));
+        p[i] = pv;
+    }
 }
 
 // model[sub] += sign * gain * x, in float32 as the reference does (main.py:483, 498).
@@ -163,13 +199,28 @@ __global__ void __launch_bounds__(kRedThreads)
 region_partials(const float *__restrict__ img, int pitch, int rows, int cols, int off_r, int off_c,
                 const double *__restrict__ mean_in, double *__restrict__ partials) {
     const double mean = mean_in ? mean_in[0] / ((double)rows * cols) : 0.0;
+    const float mean_f = (float)mean;
     const size_t total = (size_t)rows * cols;
     double s = 0.0;
+    // float32 partials over runs of up to four elements per thread, float64 across runs
+    float part = 0.0f;
+    int run = 0;
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
         const int r = (int)(i / cols), c = (int)(i - (size_t)r * cols);
-        const double v = (double)img[(size_t)(r + off_r) * pitch + c + off_c];
-        s += mean_in ? (v - mean) * (v - mean) : v;
+        const float v = img[(size_t)(r + off_r) * pitch + c + off_c];
+        if (mean_in) {
+            const float dv = __fsub_rn(v, mean_f);
+            part = __fmaf_rn(dv, dv, part);
+        } else {
+            part = __fadd_rn(part, v);
+        }
+        if (++run == 4) {
+            s += (double)part;
+            part = 0.0f;
+            run = 0;
+        }
     }
+    s += (double)part;
     s = block_sum(s);
     if (threadIdx.x == 0) {
         partials[2 * blockIdx.x] = s;
@@ -195,10 +246,13 @@ constexpr size_t kPartialBytes = 2 * kRedGrid * sizeof(double);
 
 int dual_reduce(const float *a, const float *b, const float *c, const float *d, size_t n, bool diff, double *out,
                 double *partials, cudaStream_t st) {
+    if (n % 4 || !aligned16(a) || !aligned16(b) || !aligned16(c) || !aligned16(d))
+        return set_error(MSN_ERR_INVALID, "reduction: length must be a multiple of 4 and pointers 16-byte aligned");
+    const float4 *a4 = (const float4 *)a, *b4 = (const float4 *)b, *c4 = (const float4 *)c, *d4 = (const float4 *)d;
     if (diff)
-        dual_partials<true><<<kRedGrid, kRedThreads, 0, st>>>(a, b, c, d, n, partials);
+        dual_partials<true><<<kRedGrid, kRedThreads, 0, st>>>(a4, b4, c4, d4, n / 4, partials);
     else
-        dual_partials<false><<<kRedGrid, kRedThreads, 0, st>>>(a, b, c, d, n, partials);
+        dual_partials<false><<<kRedGrid, kRedThreads, 0, st>>>(a4, b4, c4, d4, n / 4, partials);
     MSN_TRY(check_launch("dual_partials"));
     finalize_pairs<<<1, 1024, 0, st>>>(partials, out);
     return check_launch("finalize_pairs");
@@ -237,8 +291,11 @@ extern "C" int msn_cg_alpha_x(const float *d_x, const float *d_p, double *d_scal
                               int *d_neg_count, void *stream) {
     clear_error();
     if (!d_x || !d_p || !d_scal || !d_xn || !d_neg_count) return set_error(MSN_ERR_INVALID, "msn_cg_alpha_x: null pointer");
+    if (n % 4 || !aligned16(d_x) || !aligned16(d_p) || !aligned16(d_xn))
+        return set_error(MSN_ERR_INVALID, "msn_cg_alpha_x: length must be a multiple of 4, pointers 16-byte aligned");
     MSN_TRY(check_cuda(cudaMemsetAsync(d_neg_count, 0, sizeof(int), as_stream(stream)), "reset count"));
-    cg_alpha_x<<<ew_grid(n), 256, 0, as_stream(stream)>>>(d_x, d_p, d_scal, d_xn, n, d_neg_count);
+    cg_alpha_x<<<ew_grid(n / 4), 256, 0, as_stream(stream)>>>((const float4 *)d_x, (const float4 *)d_p, d_scal,
+                                                             (float4 *)d_xn, n / 4, d_neg_count);
     return check_launch("cg_alpha_x");
 }
 
@@ -255,9 +312,12 @@ extern "C" int msn_cg_residual(const float *d_r, const float *d_ap, double *d_sc
     clear_error();
     if (!d_r || !d_ap || !d_scal || !d_rn) return set_error(MSN_ERR_INVALID, "msn_cg_residual: null pointer");
     MSN_TRY(check_red_ws(d_work, work_bytes, "msn_cg_residual"));
+    if (n % 4 || !aligned16(d_r) || !aligned16(d_ap) || !aligned16(d_rn))
+        return set_error(MSN_ERR_INVALID, "msn_cg_residual: length must be a multiple of 4, pointers 16-byte aligned");
     cudaStream_t st = as_stream(stream);
     double *partials = (double *)d_work;
-    cg_residual<<<kRedGrid, kRedThreads, 0, st>>>(d_r, d_ap, d_scal, d_rn, n, partials);
+    cg_residual<<<kRedGrid, kRedThreads, 0, st>>>((const float4 *)d_r, (const float4 *)d_ap, d_scal, (float4 *)d_rn,
+                                                  n / 4, partials);
     MSN_TRY(check_launch("cg_residual"));
     finalize_pairs<<<1, 1024, 0, st>>>(partials, d_scal + S_RNRN);   // writes S_RNRN and S_RNRN+1 (= S_BETA, overwritten next)
     MSN_TRY(check_launch("finalize_pairs"));
@@ -268,7 +328,9 @@ extern "C" int msn_cg_residual(const float *d_r, const float *d_ap, double *d_sc
 extern "C" int msn_cg_direction(const float *d_rn, float *d_p, const double *d_scal, size_t n, void *stream) {
     clear_error();
     if (!d_rn || !d_p || !d_scal) return set_error(MSN_ERR_INVALID, "msn_cg_direction: null pointer");
-    cg_direction<<<ew_grid(n), 256, 0, as_stream(stream)>>>(d_rn, d_p, d_scal, n);
+    if (n % 4 || !aligned16(d_rn) || !aligned16(d_p))
+        return set_error(MSN_ERR_INVALID, "msn_cg_direction: length must be a multiple of 4, pointers 16-byte aligned");
+    cg_direction<<<ew_grid(n / 4), 256, 0, as_stream(stream)>>>((const float4 *)d_rn, (float4 *)d_p, d_scal, n / 4);
     return check_launch("cg_direction");
 }
 

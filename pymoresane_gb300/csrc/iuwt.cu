@@ -22,7 +22,7 @@
 namespace msn {
 namespace {
 
-enum Epilogue { kStore = 0, kDetail = 1, kAdd = 2 };
+enum Epilogue { kStore = 0, kDetail = 1, kAdd = 2, kDetailMask = 3 };
 
 constexpr int kThreads = 256;
 constexpr int kMaxSmem = 200 * 1024;
@@ -86,7 +86,7 @@ __device__ __forceinline__ float4 horizontal4(const float *__restrict__ s, int c
 template <int EPI>
 __global__ void __launch_bounds__(kThreads)
 atrous_band(const float *__restrict__ in, float *__restrict__ out, const float *__restrict__ aux,
-            int ny, int nx, int d, int band_rows) {
+            const float *__restrict__ mask, int ny, int nx, int d, int band_rows) {
     extern __shared__ float4 smem4[];
     const float *band = reinterpret_cast<const float *>(smem4);
     const int r0 = blockIdx.x * band_rows;
@@ -122,11 +122,18 @@ atrous_band(const float *__restrict__ in, float *__restrict__ out, const float *
         float4 x;
         if (EPI != kStore) x = __ldg(aux4 + g4);
         float4 v = horizontal4(band + rr * nx, c4 * 4, nx, d);
-        if (EPI == kDetail) {
+        if (EPI == kDetail || EPI == kDetailMask) {
             v.x = __fsub_rn(x.x, v.x);
             v.y = __fsub_rn(x.y, v.y);
             v.z = __fsub_rn(x.z, v.z);
             v.w = __fsub_rn(x.w, v.w);
+        }
+        if (EPI == kDetailMask) {  // mask * detail, as the reference's separate product (main.py:383)
+            const float4 m = __ldg(reinterpret_cast<const float4 *>(mask) + g4);
+            v.x = __fmul_rn(v.x, m.x);
+            v.y = __fmul_rn(v.y, m.y);
+            v.z = __fmul_rn(v.z, m.z);
+            v.w = __fmul_rn(v.w, m.w);
         }
         if (EPI == kAdd) {
             v.x = __fadd_rn(v.x, x.x);
@@ -163,7 +170,8 @@ int band_rows_for(int ny, int nx) {
 }
 
 template <int EPI>
-int launch_band(const float *in, float *out, const float *aux, int ny, int nx, int d, cudaStream_t st) {
+int launch_band(const float *in, float *out, const float *aux, int ny, int nx, int d, cudaStream_t st,
+                const float *mask = nullptr) {
     static std::once_flag once;
     std::call_once(once, [] {
         cudaFuncSetAttribute(atrous_band<EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxSmem);
@@ -171,7 +179,7 @@ int launch_band(const float *in, float *out, const float *aux, int ny, int nx, i
     const int band = band_rows_for(ny, nx);
     const size_t smem = (size_t)band * nx * sizeof(float);
     const int grid = (ny + band - 1) / band;
-    atrous_band<EPI><<<grid, kThreads, smem, st>>>(in, out, aux, ny, nx, d, band);
+    atrous_band<EPI><<<grid, kThreads, smem, st>>>(in, out, aux, mask, ny, nx, d, band);
     return check_launch("atrous_band");
 }
 
@@ -214,9 +222,13 @@ int iuwt_smooth_detail(const float *in, const float *c0, float *w, int ny, int n
 int iuwt_smooth_add(const float *in, const float *w, float *out, int ny, int nx, int scale, cudaStream_t st) {
     return launch_band<kAdd>(in, out, w, ny, nx, 1 << scale, st);
 }
+int iuwt_smooth_detail_mask(const float *in, const float *c0, const float *mask, float *w, int ny, int nx, int scale,
+                            cudaStream_t st) {
+    return launch_band<kDetailMask>(in, w, c0, ny, nx, 1 << scale, st, mask);
+}
 
 int iuwt_decompose_impl(const float *d_in, float *d_detail, float *d_smoothed, int ny, int nx, int scale_count,
-                        int scale_adjust, float *p0, float *p1, cudaStream_t st) {
+                        int scale_adjust, float *p0, float *p1, cudaStream_t st, const float *d_mask = nullptr) {
     const size_t plane = (size_t)ny * nx;
     float *bufs[2] = {p0, p1};
     const float *cur = d_in;
@@ -233,7 +245,11 @@ int iuwt_decompose_impl(const float *d_in, float *d_detail, float *d_smoothed, i
         const int nb = next();
         float *c = (last && d_smoothed) ? d_smoothed : bufs[nb];
         MSN_TRY(iuwt_smooth(cur, c, ny, nx, s, st));
-        MSN_TRY(iuwt_smooth_detail(c, cur, d_detail + (size_t)(s - scale_adjust) * plane, ny, nx, s, st));
+        float *w = d_detail + (size_t)(s - scale_adjust) * plane;
+        if (d_mask)
+            MSN_TRY(iuwt_smooth_detail_mask(c, cur, d_mask + (size_t)(s - scale_adjust) * plane, w, ny, nx, s, st));
+        else
+            MSN_TRY(iuwt_smooth_detail(c, cur, w, ny, nx, s, st));
         cur = c;
         cur_buf = (c == d_smoothed) ? -1 : nb;
     }
@@ -325,6 +341,25 @@ extern "C" int msn_iuwt_decompose(const float *d_in, float *d_detail, float *d_s
     MSN_TRY(split_workspace(d_work, work_bytes, ny, nx, &p0, &p1, fn));
     return iuwt_decompose_impl(d_in, d_detail, d_smoothed, ny, nx, scale_count, scale_adjust, p0, p1,
                                as_stream(stream));
+}
+
+extern "C" int msn_iuwt_decompose_masked(const float *d_in, const float *d_mask, float *d_detail, int ny, int nx,
+                                         int scale_count, int scale_adjust, void *d_work, size_t work_bytes,
+                                         void *stream) {
+    clear_error();
+    static const char *fn = "msn_iuwt_decompose_masked";
+    MSN_TRY(validate_image(ny, nx, fn));
+    MSN_TRY(validate_scales(ny, nx, scale_count, fn));
+    if (scale_adjust < 0 || scale_adjust > scale_count)
+        return set_error(MSN_ERR_INVALID, "%s: scale_adjust=%d outside [0, %d]", fn, scale_adjust, scale_count);
+    if (!d_in || !d_mask || (scale_count > scale_adjust && !d_detail))
+        return set_error(MSN_ERR_INVALID, "%s: null input, mask or detail pointer", fn);
+    if (!aligned16(d_in) || !aligned16(d_detail) || !aligned16(d_mask))
+        return set_error(MSN_ERR_INVALID, "%s: device pointers must be 16-byte aligned", fn);
+    float *p0, *p1;
+    MSN_TRY(split_workspace(d_work, work_bytes, ny, nx, &p0, &p1, fn));
+    return iuwt_decompose_impl(d_in, d_detail, nullptr, ny, nx, scale_count, scale_adjust, p0, p1, as_stream(stream),
+                               d_mask);
 }
 
 extern "C" int msn_iuwt_recompose(const float *d_detail, int planes, const float *d_smoothed, float *d_out, int ny,

@@ -17,7 +17,13 @@ void clear_error();
 // Checks the result of a CUDA runtime call / kernel launch.
 int check_cuda(cudaError_t e, const char *what);
 
-inline int check_launch(const char *what) { return check_cuda(cudaGetLastError(), what); }
+// Counts every kernel launch of the library (read with msn_launch_count).
+void count_launch();
+
+inline int check_launch(const char *what) {
+    count_launch();
+    return check_cuda(cudaGetLastError(), what);
+}
 
 inline cudaStream_t as_stream(void *s) { return reinterpret_cast<cudaStream_t>(s); }
 

@@ -66,6 +66,20 @@ def iuwt_decompose(x, scale_count, scale_adjust=0, store_smoothed=False, out=Non
     return out, sm
 
 
+def iuwt_decompose_masked(x, mask, scale_count, scale_adjust=0, out=None, work=None):
+    """mask * detail stack, the mask applied inside the detail pass."""
+    x = as_f32_cuda(x)
+    ny, nx = x.shape
+    planes = scale_count - scale_adjust
+    if out is None:
+        out = torch.empty((max(planes, 0), ny, nx), dtype=torch.float32, device=x.device)
+    if work is None:
+        work = iuwt_workspace(ny, nx, x.device)
+    _native.call("msn_iuwt_decompose_masked", x.data_ptr(), mask.data_ptr(), out.data_ptr() if planes > 0 else None,
+                 ny, nx, scale_count, scale_adjust, work.data_ptr(), work.numel(), stream_handle())
+    return out
+
+
 def iuwt_recompose(w, scale_adjust=0, smoothed=None, out=None, work=None):
     """Inverse transform of a detail stack [planes, ny, nx] (+ optional smoothest plane)."""
     w = as_f32_cuda(w)

@@ -78,45 +78,32 @@ class _Buffers:
         self.fmax = torch.empty(1, dtype=torch.float32, device=device)
 
 
-class DataImage(object):
-    """MORESANE on one dirty image / PSF pair (pymoresane/main.py:18-676)."""
+class Deconvolver:
+    """Device-resident MORESANE for one PSF (and optional mask) on the current CUDA device.
 
-    def __init__(self, dirty_data, psf_data, mask_data, cdelt1, cdelt2):
-        self.dirty_data = np.asarray(dirty_data).astype(np.float32)
-        self.psf_data = np.asarray(psf_data).astype(np.float32)
-        self.mask_name = None if mask_data is None else getattr(self, "mask_name", "mask")
-        self.mask = None if mask_data is None else np.asarray(mask_data)
-        self.dirty_data_shape = self.dirty_data.shape
-        self.psf_data_shape = self.psf_data.shape
-        self.complete = False
-        self.model = np.zeros_like(self.dirty_data)
-        self.residual = np.copy(self.dirty_data)
-        self.restored = np.zeros_like(self.dirty_data)
-        self.cdelt1 = cdelt1
-        self.cdelt2 = cdelt2
+    ``psf`` and ``mask`` are CUDA tensors (or arrays, uploaded once); the PSF
+    spectra, PSF scale energies and every work buffer are built on first use
+    and kept for later calls. ``moresane(dirty, ...)`` takes a CUDA tensor and
+    returns device tensors, so a caller can keep whole deconvolutions on the
+    GPU; DataImage wraps it with the reference's host-array interface.
+    """
+
+    def __init__(self, psf, mask=None, dirty_shape=None):
+        dev.require_cuda()
+        _native.load()
+        self.device = torch.device("cuda", torch.cuda.current_device())
+        self.psf = dev.as_f32_cuda(psf, device=self.device)
+        self.mask = None if mask is None else dev.as_f32_cuda(mask, device=self.device)
+        self.psf_data_shape = tuple(self.psf.shape)
+        self.dirty_data_shape = dirty_shape
         self.log = []
+        self.complete = False
         self._psf_cache = _PsfCache()
         self._bufs = {}
-        self._dev = None
-
-    # ------------------------------------------------------------------ device state
-    def _device_inputs(self):
-        if self._dev is None:
-            dev.require_cuda()
-            _native.load()
-            d = torch.device("cuda", torch.cuda.current_device())
-            self._dev = {
-                "psf": torch.from_numpy(np.ascontiguousarray(self.psf_data)).to(d),
-                "mask": None if self.mask is None else torch.from_numpy(
-                    np.ascontiguousarray(self.mask, dtype=np.float32)).to(d),
-                "device": d,
-            }
-        return self._dev
 
     def _spectra(self, subregion, conv_mode):
         """(spec_sub, spec_data, psf_subregion) per pymoresane/main.py:118-213 (GPU branches)."""
-        devs = self._device_inputs()
-        psf = devs["psf"]
+        psf = self.psf
         n = self.dirty_data_shape[0]
         p0 = self.psf_data_shape[0]
         double = all(p == 2 * d for p, d in zip(self.psf_data_shape, self.dirty_data_shape))
@@ -154,7 +141,7 @@ class DataImage(object):
                 raise ValueError(f"unknown conv_mode {conv_mode!r}")
             return spec_sub, spec_data, psf_sub
 
-        return self._psf_cache.get((subregion, conv_mode), build)
+        return self._psf_cache.get((n, subregion, conv_mode), build)
 
     def _energies(self, psf_sub, scale_count, bufs):
         """||w_s||_2 of the PSF-subregion decomposition, as float32 (pymoresane/main.py:221-226)."""
@@ -169,70 +156,25 @@ class DataImage(object):
         return self._psf_cache.get(("energies", psf_sub.data_ptr(), scale_count), build)
 
     def _buffers(self, ns, scale_count, spec_sub, spec_data):
-        key = (ns, scale_count, spec_sub.m, spec_data.m)
+        key = (self.dirty_data_shape[0], ns, scale_count, spec_sub.m, spec_data.m)
         if key not in self._bufs:
             self._bufs = {key: _Buffers(ns, self.dirty_data_shape[0], spec_sub.m, spec_data.m, scale_count,
-                                        self._device_inputs()["device"])}
+                                        self.device)}
         return self._bufs[key]
 
-    # ------------------------------------------------------------------ algorithm
-    def moresane(self, subregion=None, scale_count=None, sigma_level=4, loop_gain=0.1, tolerance=0.75, accuracy=1e-6,
-                 major_loop_miter=100, minor_loop_miter=30, all_on_gpu=False, decom_mode="gpu", core_count=1,
-                 conv_device='gpu', conv_mode='linear', extraction_mode='gpu', enforce_positivity=False,
-                 edge_suppression=False, edge_offset=0, flux_threshold=0, neg_comp=False, edge_excl=0, int_excl=0):
-        """MORESANE deconvolution (pymoresane/main.py:53-521); updates self.model and self.residual."""
-        _check_modes(all_on_gpu, decom_mode, conv_device, extraction_mode)
-        devs = self._device_inputs()
-        dirty = torch.from_numpy(np.ascontiguousarray(self.dirty_data)).to(devs["device"])
-        model, residual, major = self._moresane_device(
-            dirty, subregion, scale_count, sigma_level, loop_gain, tolerance, accuracy, major_loop_miter,
-            minor_loop_miter, conv_mode, enforce_positivity, edge_suppression, edge_offset, flux_threshold,
-            neg_comp, edge_excl, int_excl)
-        if major > 0:
-            self.model += model.cpu().numpy()
-            self.residual = residual.cpu().numpy()
-        return major
+    def moresane(self, dirty, subregion=None, scale_count=None, sigma_level=4, loop_gain=0.1, tolerance=0.75,
+                 accuracy=1e-6, major_loop_miter=100, minor_loop_miter=30, conv_mode='linear',
+                 enforce_positivity=False, edge_suppression=False, edge_offset=0, flux_threshold=0, neg_comp=False,
+                 edge_excl=0, int_excl=0):
+        """One MORESANE run (pymoresane/main.py:99-521) on the device image ``dirty``.
 
-    def moresane_by_scale(self, start_scale=1, stop_scale=20, subregion=None, sigma_level=4, loop_gain=0.1,
-                          tolerance=0.75, accuracy=1e-6, major_loop_miter=100, minor_loop_miter=30, all_on_gpu=False,
-                          decom_mode="gpu", core_count=1, conv_device='gpu', conv_mode='linear',
-                          extraction_mode='gpu', enforce_positivity=False, edge_suppression=False, edge_offset=0,
-                          flux_threshold=0, neg_comp=False, edge_excl=0, int_excl=0):
-        """Scale-by-scale MORESANE (pymoresane/main.py:523-599), residual kept on the device between scales."""
-        _check_modes(all_on_gpu, decom_mode, conv_device, extraction_mode)
-        devs = self._device_inputs()
-        d = devs["device"]
-        dirty = torch.from_numpy(np.ascontiguousarray(self.dirty_data)).to(d)
-        model_acc = torch.from_numpy(np.ascontiguousarray(self.model)).to(d)
-        residual = torch.from_numpy(np.ascontiguousarray(self.residual)).to(d)
-        n = self.dirty_data_shape[0]
-        st = dev.stream_handle()
-        scale_count = start_scale
+        Returns (model, residual, major_iterations) as CUDA tensors (residual
+        is None when no major iteration ran); sets ``self.complete`` when the
+        run did no work, as the reference does.
+        """
+        dirty = dev.as_f32_cuda(dirty, device=self.device)
+        self.dirty_data_shape = tuple(dirty.shape)
         self.complete = False
-        while not self.complete:
-            logger.info("MORESANE at scale %d", scale_count)
-            model, res, major = self._moresane_device(
-                dirty, subregion, scale_count, sigma_level, loop_gain, tolerance, accuracy, major_loop_miter,
-                minor_loop_miter, conv_mode, enforce_positivity, edge_suppression, edge_offset, flux_threshold,
-                neg_comp, edge_excl, int_excl)
-            if major > 0:
-                _native.call("msn_model_update", model_acc.data_ptr(), n, model.data_ptr(), n, 0, 0, 1.0, 1, st)
-                residual = res
-            dirty = residual
-            scale_count += 1
-            if scale_count > (np.log2(n)) - 1:
-                logger.info("Maximum scale reached - finished.")
-                break
-            if scale_count > stop_scale:
-                logger.info("Maximum scale reached - finished.")
-                break
-        self.model = model_acc.cpu().numpy()
-        self.residual = residual.cpu().numpy()
-        self.complete = False
-
-    def _moresane_device(self, dirty, subregion, scale_count, sigma_level, loop_gain, tolerance, accuracy,
-                         major_loop_miter, minor_loop_miter, conv_mode, enforce_positivity, edge_suppression,
-                         edge_offset, flux_threshold, neg_comp, edge_excl, int_excl):
         n = self.dirty_data_shape[0]
         if n % 2 == 1:
             logger.error("Image size is uneven. Please use even dimensions.")
@@ -252,8 +194,8 @@ class DataImage(object):
         V = B.vec
         nvec = ns * ns
         mask_sub = None
-        if self._dev["mask"] is not None:
-            mask_sub = self._dev["mask"][o:o + ns, o:o + ns].contiguous()
+        if self.mask is not None:
+            mask_sub = self.mask[o:o + ns, o:o + ns].contiguous()
 
         supp = None
         if edge_suppression or edge_offset > 0:
@@ -275,8 +217,7 @@ class DataImage(object):
         def apply_a(vec_in, vec_out, max_scale, adj, planes):
             dev.fft_convolve(vec_in, spec_sub, linear, out=V["tmp"], work=B.fft_work)
             w = B.planes[:planes]
-            dev.iuwt_decompose(V["tmp"], max_scale, adj, out=w, work=B.iuwt_work)
-            call("msn_mul", w.data_ptr(), B.emask.data_ptr(), w.data_ptr(), w.numel(), st)
+            dev.iuwt_decompose_masked(V["tmp"], B.emask, max_scale, adj, out=w, work=B.iuwt_work)
             dev.iuwt_recompose(w, adj, out=vec_out, work=B.iuwt_work)
 
         def residual_of(model):
@@ -355,8 +296,7 @@ class DataImage(object):
                     # model_sources = mask * W(H xn); snr against the extracted sources
                     dev.fft_convolve(xn, spec_sub, linear, out=V["tmp"], work=B.fft_work)
                     w = B.planes[:planes]
-                    dev.iuwt_decompose(V["tmp"], max_scale, scale_adjust, out=w, work=B.iuwt_work)
-                    call("msn_mul", w.data_ptr(), B.emask.data_ptr(), w.data_ptr(), w.numel(), st)
+                    dev.iuwt_decompose_masked(V["tmp"], B.emask, max_scale, scale_adjust, out=w, work=B.iuwt_work)
                     dev.snr_sums(B.esrc[:planes].reshape(-1), w.reshape(-1), out=B.snr2, work=B.red_work)
                     s2 = B.snr2.cpu().numpy()
                     snr_last = snr_current
@@ -420,6 +360,93 @@ class DataImage(object):
                 self.complete = True
                 break
         return model, residual, major
+
+
+
+class DataImage(object):
+    """MORESANE on one dirty image / PSF pair with host arrays (pymoresane/main.py:18-676)."""
+
+    def __init__(self, dirty_data, psf_data, mask_data, cdelt1, cdelt2):
+        self.dirty_data = np.asarray(dirty_data).astype(np.float32)
+        self.psf_data = np.asarray(psf_data).astype(np.float32)
+        self.mask_name = None if mask_data is None else getattr(self, "mask_name", "mask")
+        self.mask = None if mask_data is None else np.asarray(mask_data)
+        self.dirty_data_shape = self.dirty_data.shape
+        self.psf_data_shape = self.psf_data.shape
+        self.complete = False
+        self.model = np.zeros_like(self.dirty_data)
+        self.residual = np.copy(self.dirty_data)
+        self.restored = np.zeros_like(self.dirty_data)
+        self.cdelt1 = cdelt1
+        self.cdelt2 = cdelt2
+        self._engine = None
+
+    @property
+    def engine(self):
+        if self._engine is None:
+            mask = None if self.mask is None else np.ascontiguousarray(self.mask, dtype=np.float32)
+            self._engine = Deconvolver(np.ascontiguousarray(self.psf_data), mask, self.dirty_data_shape)
+        return self._engine
+
+    @property
+    def log(self):
+        return self.engine.log
+
+    def moresane(self, subregion=None, scale_count=None, sigma_level=4, loop_gain=0.1, tolerance=0.75, accuracy=1e-6,
+                 major_loop_miter=100, minor_loop_miter=30, all_on_gpu=False, decom_mode="gpu", core_count=1,
+                 conv_device='gpu', conv_mode='linear', extraction_mode='gpu', enforce_positivity=False,
+                 edge_suppression=False, edge_offset=0, flux_threshold=0, neg_comp=False, edge_excl=0, int_excl=0):
+        """MORESANE deconvolution (pymoresane/main.py:53-521); updates self.model and self.residual."""
+        _check_modes(all_on_gpu, decom_mode, conv_device, extraction_mode)
+        eng = self.engine
+        dirty = torch.from_numpy(np.ascontiguousarray(self.dirty_data)).to(eng.device)
+        model, residual, major = eng.moresane(
+            dirty, subregion, scale_count, sigma_level, loop_gain, tolerance, accuracy, major_loop_miter,
+            minor_loop_miter, conv_mode, enforce_positivity, edge_suppression, edge_offset, flux_threshold,
+            neg_comp, edge_excl, int_excl)
+        self.complete = eng.complete
+        if major > 0:
+            self.model += model.cpu().numpy()
+            self.residual = residual.cpu().numpy()
+        return major
+
+    def moresane_by_scale(self, start_scale=1, stop_scale=20, subregion=None, sigma_level=4, loop_gain=0.1,
+                          tolerance=0.75, accuracy=1e-6, major_loop_miter=100, minor_loop_miter=30, all_on_gpu=False,
+                          decom_mode="gpu", core_count=1, conv_device='gpu', conv_mode='linear',
+                          extraction_mode='gpu', enforce_positivity=False, edge_suppression=False, edge_offset=0,
+                          flux_threshold=0, neg_comp=False, edge_excl=0, int_excl=0):
+        """Scale-by-scale MORESANE (pymoresane/main.py:523-599), residual kept on the device between scales."""
+        _check_modes(all_on_gpu, decom_mode, conv_device, extraction_mode)
+        eng = self.engine
+        d = eng.device
+        dirty = torch.from_numpy(np.ascontiguousarray(self.dirty_data)).to(d)
+        model_acc = torch.from_numpy(np.ascontiguousarray(self.model)).to(d)
+        residual = torch.from_numpy(np.ascontiguousarray(self.residual)).to(d)
+        n = self.dirty_data_shape[0]
+        st = dev.stream_handle()
+        scale_count = start_scale
+        self.complete = False
+        while not self.complete:
+            logger.info("MORESANE at scale %d", scale_count)
+            model, res, major = eng.moresane(
+                dirty, subregion, scale_count, sigma_level, loop_gain, tolerance, accuracy, major_loop_miter,
+                minor_loop_miter, conv_mode, enforce_positivity, edge_suppression, edge_offset, flux_threshold,
+                neg_comp, edge_excl, int_excl)
+            self.complete = eng.complete
+            if major > 0:
+                _native.call("msn_model_update", model_acc.data_ptr(), n, model.data_ptr(), n, 0, 0, 1.0, 1, st)
+                residual = res
+            dirty = residual
+            scale_count += 1
+            if scale_count > (np.log2(n)) - 1:
+                logger.info("Maximum scale reached - finished.")
+                break
+            if scale_count > stop_scale:
+                logger.info("Maximum scale reached - finished.")
+                break
+        self.model = model_acc.cpu().numpy()
+        self.residual = residual.cpu().numpy()
+        self.complete = False
 
     # ------------------------------------------------------------------ outputs
     def save_fits(self, data, name):

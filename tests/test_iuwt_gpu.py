@@ -131,3 +131,15 @@ def test_full_size_rows_match_f32_oracle(cuda):
     d = G.iuwt_decomposition(x, 8, 0, mode="gpu")
     od = O.decompose(x, 8, 0, arith="f32fma")
     assert np.array_equal(d, od)
+
+
+@pytest.mark.parametrize("shape,scales,adj", [((64, 64), 4, 0), ((128, 96), 5, 2)])
+def test_masked_decomposition_equals_product(cuda, shape, scales, adj):
+    # msn_iuwt_decompose_masked == mask * msn_iuwt_decompose, bit for bit (main.py:381-383)
+    x = torch.from_numpy(rand(shape, 7)).cuda()
+    rng = np.random.default_rng(8)
+    mask = torch.from_numpy((rng.random((scales - adj,) + shape) < 0.3).astype(np.float32)).cuda()
+    w, _ = dev.iuwt_decompose(x, scales, adj)
+    got = dev.iuwt_decompose_masked(x, mask, scales, adj)
+    want = w * mask
+    assert torch.equal(got.view(torch.int32), want.view(torch.int32))
