@@ -1,18 +1,20 @@
 // Shared-memory Stockham FFT core (mixed radix 2, 3, 4, 8, 16) for sm_103a.
 //
 // A "team" of M/E threads transforms one complex sequence of length M held in
-// shared memory; every thread keeps E elements in registers per pass. Each
-// pass of radix R performs the Stockham autosort step (Govindaraju et al.,
-// "High performance discrete Fourier transforms on graphics processors",
+// shared memory; every thread keeps E elements (16 for M = 2^a, 24 for
+// M = 3 * 2^a) in registers per pass, i.e. E/R independent radix-R butterflies.
+// Each pass of radix R performs the Stockham autosort step (Govindaraju et
+// al., "High performance discrete Fourier transforms on graphics processors",
 // SC 2008): butterfly j reads x[j + r M/R], applies the twiddles
-// w^(r (j mod Ns)) with w = exp(-+2 pi i / (Ns R)), transforms the R values
-// in registers and writes them to (j div Ns) Ns R + (j mod Ns) + r Ns.
-// Output is in natural order. Shared-memory indices are padded by one
-// element every 16 (sidx) to keep the strided first pass conflict-free.
+// w^(r (j mod Ns)) with w = exp(-+2 pi i / (Ns R)), transforms the R values in
+// registers and writes them to (j div Ns) Ns R + (j mod Ns) + r Ns. Any order
+// of the radices gives the natural-order transform (the passes themselves are
+// in fft_kernels.cuh). Shared-memory indices are padded by one element every
+// 16 (sidx) to keep strided passes free of bank conflicts.
 //
-// Twiddles come from kTwiddle, a table of exp(-2 pi i k / kTwN) rounded from
-// float64 to float32 at build time (msn_twiddles.inc, generated by build.py);
-// kTwN = 2^13 * 3 covers every supported length M = 2^a or 3 * 2^a.
+// Twiddles: kTwiddle is exp(-2 pi i k / kTwN) rounded from float64 to float32
+// at build time (msn_twiddles.inc, generated by build.py); kTwN = 2^13 * 3
+// covers every supported length.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -24,12 +26,29 @@ constexpr int kTwN = 24576;
 __device__ __forceinline__ int sidx(int i) { return i + (i >> 4); }
 __host__ __device__ constexpr int padded_len(int m) { return m + (m >> 4) + 4; }
 
+// Asynchronous global -> shared copies (cp.async); with valid == false the
+// destination is zero-filled and nothing is read.
+__device__ __forceinline__ void cp_async8(void *smem_dst, const void *gmem_src, bool valid) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(smem_dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(d), "l"(gmem_src), "r"(valid ? 8 : 0)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async4(void *smem_dst, const void *gmem_src, bool valid) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(smem_dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(d), "l"(gmem_src), "r"(valid ? 4 : 0)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
 __device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
 __device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
 __device__ __forceinline__ float2 cmul(float2 a, float2 b) {
     return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
-__device__ __forceinline__ float2 cscale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
 __device__ __forceinline__ float2 cconj(float2 a) { return make_float2(a.x, -a.y); }
 
 // Multiply by -i (forward) or +i (inverse).
@@ -122,14 +141,14 @@ __device__ __forceinline__ void dft16(float2 *v) {
     dft4s<INV, 4, 1>(v);
     dft4s<INV, 8, 1>(v);
     dft4s<INV, 12, 1>(v);
-    // slot 4 k1 + k2 holds X[k1 + 4 k2]: transpose to natural order.
-    float2 t[16];
-#pragma unroll
-    for (int k1 = 0; k1 < 4; ++k1)
-#pragma unroll
-        for (int k2 = 0; k2 < 4; ++k2) t[k1 + 4 * k2] = v[4 * k1 + k2];
-#pragma unroll
-    for (int i = 0; i < 16; ++i) v[i] = t[i];
+    // slot 4 k1 + k2 now holds X[k1 + 4 k2]; out_slot<16> maps output index to slot.
+}
+
+// Register slot holding output X[r] after dft<INV, R>: natural order except for
+// radix 16, whose 4 x 4 decomposition leaves X[k1 + 4 k2] in slot 4 k1 + k2.
+template <int R>
+__host__ __device__ constexpr int out_slot(int r) {
+    return R == 16 ? 4 * (r & 3) + (r >> 2) : r;
 }
 
 template <bool INV, int R>
@@ -141,68 +160,8 @@ __device__ __forceinline__ void dft(float2 *v) {
     if constexpr (R == 16) dft16<INV>(v);
 }
 
-struct FftPlan {
-    int m;          // transform length
-    int npass;
-    int radix[8];
-};
-
 static __device__ const float2 kTwiddle[kTwN] = {
 #include "msn_twiddles.inc"
 };
-
-template <bool INV>
-__device__ __forceinline__ float2 twiddle(int idx) {
-    const float2 w = __ldg(&kTwiddle[idx]);
-    return INV ? cconj(w) : w;
-}
-
-// One Stockham pass of radix R over a team's sequence (all CTA threads call it).
-template <bool INV, int E, int R>
-__device__ __forceinline__ void fft_pass(float2 *buf, int m, int ns, int t) {
-    if constexpr (E % R == 0) {
-        constexpr int NB = E / R;
-        const int team = m / E;
-        const int stride = m / R;
-        float2 v[E];
-#pragma unroll
-        for (int b = 0; b < NB; ++b) {
-            const int j = t + b * team;
-#pragma unroll
-            for (int r = 0; r < R; ++r) v[b * R + r] = buf[sidx(j + r * stride)];
-        }
-        __syncthreads();
-#pragma unroll
-        for (int b = 0; b < NB; ++b) {
-            const int j = t + b * team;
-            const int k = j % ns;
-            if (ns > 1) {
-                const int step = kTwN / (ns * R);
-#pragma unroll
-                for (int r = 1; r < R; ++r) v[b * R + r] = cmul(v[b * R + r], twiddle<INV>(r * k * step));
-            }
-            dft<INV, R>(v + b * R);
-            const int base = (j - k) * R + k;
-#pragma unroll
-            for (int r = 0; r < R; ++r) buf[sidx(base + r * ns)] = v[b * R + r];
-        }
-        __syncthreads();
-    }
-}
-
-// Full transform of one team's sequence (unnormalised; INV uses exp(+2 pi i/M)).
-template <bool INV, int E>
-__device__ __forceinline__ void fft_team(float2 *buf, const FftPlan &p, int t) {
-    int ns = 1;
-    for (int q = 0; q < p.npass; ++q) {
-        const int r = p.radix[q];
-        if (r == 16) fft_pass<INV, E, 16>(buf, p.m, ns, t);
-        else if (r == 8) fft_pass<INV, E, 8>(buf, p.m, ns, t);
-        else if (r == 4) fft_pass<INV, E, 4>(buf, p.m, ns, t);
-        else if (r == 3) fft_pass<INV, E, 3>(buf, p.m, ns, t);
-        else fft_pass<INV, E, 2>(buf, p.m, ns, t);
-        ns *= r;
-    }
-}
 
 }  // namespace msn
