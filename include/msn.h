@@ -215,6 +215,14 @@ int msn_dot2(const float *d_a, const float *d_b, const float *d_c, const float *
 int msn_snr_sums(const float *d_a, const float *d_b, size_t n, double *d_out2, void *d_work, size_t work_bytes,
                  void *stream);
 
+/* Running model sources for the minor-loop SNR (pymoresane/main.py:413-424):
+ * ms += alpha * q (float32, alpha = (float)scal[2]) where q = mask * W(H p) is
+ * the plane stack formed for Ap; d_out2[0] = sum e^2, d_out2[1] =
+ * sum (e - ms)^2 in float64 (e: the extracted sources). By linearity this
+ * equals recomputing mask * W(H xn) from xn = x + alpha p. */
+int msn_snr_update(const float *d_e, float *d_ms, const float *d_q, const double *d_scal, size_t n, double *d_out2,
+                   void *d_work, size_t work_bytes, void *stream);
+
 /* alpha = scal[0] / scal[1] -> scal[2]; xn = x + alpha p; *d_neg_count = #(xn < 0)
  * (pymoresane/main.py:386-390). */
 int msn_cg_alpha_x(const float *d_x, const float *d_p, double *d_scal, float *d_xn, size_t n, int *d_neg_count,

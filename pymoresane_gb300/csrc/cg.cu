@@ -70,23 +70,65 @@ dual_partials(const float4 *__restrict__ a, const float4 *__restrict__ b, const 
     }
 }
 
-// Sums the kRedGrid partial pairs in a fixed order into out[0], out[1].
-__global__ void __launch_bounds__(1024) finalize_pairs(const double *__restrict__ partials, double *__restrict__ out) {
-    __shared__ double s[2][1024];
+// Sums the kRedGrid partial pairs in a fixed order into out[0], out[1]: one
+// warp-shuffle tree per warp, then one over the warp sums.
+constexpr int kFinalizeThreads = ((kRedGrid + 31) / 32) * 32;
+
+__global__ void __launch_bounds__(kFinalizeThreads)
+finalize_pairs(const double *__restrict__ partials, double *__restrict__ out) {
+    __shared__ double ws[2][kFinalizeThreads / 32];
     const int t = threadIdx.x;
-    s[0][t] = t < kRedGrid ? partials[2 * t] : 0.0;
-    s[1][t] = t < kRedGrid ? partials[2 * t + 1] : 0.0;
-    __syncthreads();
-    for (int off = 512; off > 0; off >>= 1) {
-        if (t < off) {
-            s[0][t] += s[0][t + off];
-            s[1][t] += s[1][t + off];
-        }
-        __syncthreads();
+    double a = t < kRedGrid ? partials[2 * t] : 0.0;
+    double b = t < kRedGrid ? partials[2 * t + 1] : 0.0;
+    for (int off = 16; off > 0; off >>= 1) {
+        a += __shfl_xor_sync(0xffffffffu, a, off);
+        b += __shfl_xor_sync(0xffffffffu, b, off);
     }
-    if (t == 0) {
-        out[0] = s[0][0];
-        out[1] = s[1][0];
+    if ((t & 31) == 0) {
+        ws[0][t >> 5] = a;
+        ws[1][t >> 5] = b;
+    }
+    __syncthreads();
+    if (t < 32) {
+        a = t < kFinalizeThreads / 32 ? ws[0][t] : 0.0;
+        b = t < kFinalizeThreads / 32 ? ws[1][t] : 0.0;
+        for (int off = 16; off > 0; off >>= 1) {
+            a += __shfl_xor_sync(0xffffffffu, a, off);
+            b += __shfl_xor_sync(0xffffffffu, b, off);
+        }
+        if (t == 0) {
+            out[0] = a;
+            out[1] = b;
+        }
+    }
+}
+
+// model_sources += alpha * Q with the partials of sum E^2 and sum (E - model_sources)^2.
+// By linearity mask * W(H (x + alpha p)) = mask * W(H x) + alpha * mask * W(H p), and
+// mask * W(H p) is the plane stack Q already formed for Ap, so the model sources of
+// pymoresane/main.py:413-416 and the norms of snr_ratio (iuwt_toolbox.py:304) come
+// from one pass instead of a convolution plus a decomposition.
+__global__ void __launch_bounds__(kRedThreads)
+snr_update(const float4 *__restrict__ e, float4 *__restrict__ ms, const float4 *__restrict__ q,
+           const double *__restrict__ scal, size_t n4, double *__restrict__ partials) {
+    const float a = (float)scal[S_ALPHA];
+    double s0 = 0.0, s1 = 0.0;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n4; i += (size_t)gridDim.x * blockDim.x) {
+        const float4 ev = __ldg(e + i), qv = __ldg(q + i);
+        float4 mv = ms[i];
+        mv.x = __fadd_rn(mv.x, __fmul_rn(a, qv.x));
+        mv.y = __fadd_rn(mv.y, __fmul_rn(a, qv.y));
+        mv.z = __fadd_rn(mv.z, __fmul_rn(a, qv.z));
+        mv.w = __fadd_rn(mv.w, __fmul_rn(a, qv.w));
+        ms[i] = mv;
+        s0 += (double)dot4(ev, ev);
+        s1 += (double)sqdiff4(ev, mv);
+    }
+    s0 = block_sum(s0);
+    s1 = block_sum(s1);
+    if (threadIdx.x == 0) {
+        partials[2 * blockIdx.x] = s0;
+        partials[2 * blockIdx.x + 1] = s1;
     }
 }
 
@@ -254,7 +296,7 @@ int dual_reduce(const float *a, const float *b, const float *c, const float *d, 
     else
         dual_partials<false><<<kRedGrid, kRedThreads, 0, st>>>(a4, b4, c4, d4, n / 4, partials);
     MSN_TRY(check_launch("dual_partials"));
-    finalize_pairs<<<1, 1024, 0, st>>>(partials, out);
+    finalize_pairs<<<1, kFinalizeThreads, 0, st>>>(partials, out);
     return check_launch("finalize_pairs");
 }
 
@@ -285,6 +327,22 @@ extern "C" int msn_snr_sums(const float *d_a, const float *d_b, size_t n, double
     MSN_TRY(check_red_ws(d_work, work_bytes, "msn_snr_sums"));
     // out[0] = sum a^2, out[1] = sum (a - b)^2
     return dual_reduce(d_a, d_a, d_b, nullptr, n, true, d_out2, (double *)d_work, as_stream(stream));
+}
+
+extern "C" int msn_snr_update(const float *d_e, float *d_ms, const float *d_q, const double *d_scal, size_t n,
+                              double *d_out2, void *d_work, size_t work_bytes, void *stream) {
+    clear_error();
+    if (!d_e || !d_ms || !d_q || !d_scal || !d_out2) return set_error(MSN_ERR_INVALID, "msn_snr_update: null pointer");
+    if (n % 4 || !aligned16(d_e) || !aligned16(d_ms) || !aligned16(d_q))
+        return set_error(MSN_ERR_INVALID, "msn_snr_update: length must be a multiple of 4, pointers 16-byte aligned");
+    MSN_TRY(check_red_ws(d_work, work_bytes, "msn_snr_update"));
+    cudaStream_t st = as_stream(stream);
+    double *partials = (double *)d_work;
+    snr_update<<<kRedGrid, kRedThreads, 0, st>>>((const float4 *)d_e, (float4 *)d_ms, (const float4 *)d_q, d_scal, n / 4,
+                                                  partials);
+    MSN_TRY(check_launch("snr_update"));
+    finalize_pairs<<<1, kFinalizeThreads, 0, st>>>(partials, d_out2);
+    return check_launch("finalize_pairs");
 }
 
 extern "C" int msn_cg_alpha_x(const float *d_x, const float *d_p, double *d_scal, float *d_xn, size_t n,
@@ -319,7 +377,7 @@ extern "C" int msn_cg_residual(const float *d_r, const float *d_ap, double *d_sc
     cg_residual<<<kRedGrid, kRedThreads, 0, st>>>((const float4 *)d_r, (const float4 *)d_ap, d_scal, (float4 *)d_rn,
                                                   n / 4, partials);
     MSN_TRY(check_launch("cg_residual"));
-    finalize_pairs<<<1, 1024, 0, st>>>(partials, d_scal + S_RNRN);   // writes S_RNRN and S_RNRN+1 (= S_BETA, overwritten next)
+    finalize_pairs<<<1, kFinalizeThreads, 0, st>>>(partials, d_scal + S_RNRN);   // writes S_RNRN and S_RNRN+1 (= S_BETA, overwritten next)
     MSN_TRY(check_launch("finalize_pairs"));
     cg_beta<<<1, 1, 0, st>>>(d_scal);
     return check_launch("cg_beta");
@@ -368,12 +426,12 @@ extern "C" int msn_region_std(const float *d_img, int pitch, int rows, int cols,
     double *partials = (double *)d_work;
     region_partials<<<kRedGrid, kRedThreads, 0, st>>>(d_img, pitch, rows, cols, off_r, off_c, nullptr, partials);
     MSN_TRY(check_launch("region_partials"));
-    finalize_pairs<<<1, 1024, 0, st>>>(partials, d_out4);
+    finalize_pairs<<<1, kFinalizeThreads, 0, st>>>(partials, d_out4);
     MSN_TRY(check_launch("finalize_pairs"));
     region_partials<<<kRedGrid, kRedThreads, 0, st>>>(d_img, pitch, rows, cols, off_r, off_c, d_out4, partials);
     MSN_TRY(check_launch("region_partials"));
     // keep the first sum: write the second pair to out[1] via a temporary slot
-    finalize_pairs<<<1, 1024, 0, st>>>(partials, d_out4 + 1);
+    finalize_pairs<<<1, kFinalizeThreads, 0, st>>>(partials, d_out4 + 1);
     MSN_TRY(check_launch("finalize_pairs"));
     std_finish<<<1, 1, 0, st>>>(d_out4, (long long)rows * cols);
     return check_launch("std_finish");

@@ -63,6 +63,7 @@ class _Buffers:
         self.emask = torch.empty((s, ns, ns), **f32)
         self.esrc = torch.empty((s, ns, ns), **f32)
         self.planes = torch.empty((s, ns, ns), **f32)
+        self.ms = torch.empty((s, ns, ns), **f32)   # running model sources mask * W(H x)
         self.vec = {k: torch.empty((ns, ns), **f32) for k in ("x", "xn", "r", "rn", "p", "ap", "tmp", "rec")}
         self.conv_full = torch.empty((n_full, n_full), **f32)
         self.iuwt_work = dev.iuwt_workspace(ns, ns, device)
@@ -98,6 +99,10 @@ class Deconvolver:
         self.dirty_data_shape = dirty_shape
         self.log = []
         self.complete = False
+        # True: keep mask * W(H x) as a running sum (ms += alpha * mask * W(H p), exact by
+        # linearity) instead of recomputing mask * W(H xn) with a convolution and a
+        # decomposition every minor iteration as pymoresane/main.py:413-416 does.
+        self.incremental_snr = True
         self._psf_cache = _PsfCache()
         self._bufs = {}
 
@@ -276,6 +281,8 @@ class Deconvolver:
 
                 x, xn, r, rn, p, ap = V["x"], V["xn"], V["r"], V["rn"], V["p"], V["ap"]
                 x.zero_()
+                if self.incremental_snr:
+                    B.ms[:planes].zero_()
                 r.copy_(V["rec"])
                 p.copy_(V["rec"])
                 minor = 0
@@ -293,11 +300,18 @@ class Deconvolver:
                     call("msn_cg_residual", r.data_ptr(), ap.data_ptr(), B.scal.data_ptr(), rn.data_ptr(), nvec,
                          B.red_work.data_ptr(), B.red_work.numel(), st)
                     call("msn_cg_direction", rn.data_ptr(), p.data_ptr(), B.scal.data_ptr(), nvec, st)
-                    # model_sources = mask * W(H xn); snr against the extracted sources
-                    dev.fft_convolve(xn, spec_sub, linear, out=V["tmp"], work=B.fft_work)
-                    w = B.planes[:planes]
-                    dev.iuwt_decompose_masked(V["tmp"], B.emask, max_scale, scale_adjust, out=w, work=B.iuwt_work)
-                    dev.snr_sums(B.esrc[:planes].reshape(-1), w.reshape(-1), out=B.snr2, work=B.red_work)
+                    # model_sources = mask * W(H xn) and the SNR against the extracted sources
+                    if self.incremental_snr:
+                        # ms += alpha * (mask * W(H p)), the plane stack left in B.planes by apply_a
+                        call("msn_snr_update", B.esrc.data_ptr(), B.ms.data_ptr(), B.planes.data_ptr(),
+                             B.scal.data_ptr(), planes * nvec, B.snr2.data_ptr(), B.red_work.data_ptr(),
+                             B.red_work.numel(), st)
+                    else:
+                        dev.fft_convolve(xn, spec_sub, linear, out=V["tmp"], work=B.fft_work)
+                        w = B.planes[:planes]
+                        dev.iuwt_decompose_masked(V["tmp"], B.emask, max_scale, scale_adjust, out=w,
+                                                  work=B.iuwt_work)
+                        dev.snr_sums(B.esrc[:planes].reshape(-1), w.reshape(-1), out=B.snr2, work=B.red_work)
                     s2 = B.snr2.cpu().numpy()
                     snr_last = snr_current
                     with np.errstate(divide="ignore", invalid="ignore"):

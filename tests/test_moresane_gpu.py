@@ -94,3 +94,25 @@ def test_errors(cuda):
         img.moresane(decom_mode="ser", conv_device="gpu", extraction_mode="gpu")
     # all_on_gpu overrides the individual modes, as in the reference (main.py:113-116)
     img.moresane(all_on_gpu=True, decom_mode="ser", conv_device="cpu", extraction_mode="cpu", major_loop_miter=1)
+
+
+@pytest.mark.parametrize("name", ["lin_double", "circ_pos", "neg_excl"])
+def test_incremental_model_sources_same_decisions(cuda, name):
+    # The running model sources (ms += alpha mask W(H p)) against the reference's direct
+    # recomputation of mask W(H xn) every minor iteration: same decisions, same model.
+    from pymoresane_gb300.main import Deconvolver
+    import torch
+    g = np.load(os.path.join(GOLDEN, "moresane.npz"))
+    pk, rk = mg.MORESANE_CASES[name]
+    kw = dict(mg.RUN_DEFAULTS, **rk)
+    dirty = torch.from_numpy(g[f"{name}_dirty"]).cuda()
+    runs = []
+    for inc in (True, False):
+        eng = Deconvolver(g[f"{name}_psf"])
+        eng.incremental_snr = inc
+        model, residual, major = eng.moresane(dirty, **kw)
+        runs.append((eng.log, model.cpu().numpy()))
+    (la, ma), (lb, mb) = runs
+    assert [(r["max_scale"], r["scale_adjust"], r["minor"]) for r in la] == \
+           [(r["max_scale"], r["scale_adjust"], r["minor"]) for r in lb]
+    assert np.max(np.abs(ma - mb)) <= MODEL_TOL * np.max(np.abs(mb))
