@@ -256,6 +256,72 @@ int msn_mul(const float *d_a, const float *d_b, float *d_out, size_t n, void *st
 int msn_region_std(const float *d_img, int pitch, int rows, int cols, int off_r, int off_c, double *d_out4,
                    void *d_work, size_t work_bytes, void *stream);
 
+/* ---------------------------------------------------------------------------
+ * Native minor loop (CUDA graph with device-side stop rules).
+ *
+ * Replaces the host-driven conjugate-gradient loop of DataImage.moresane,
+ * pymoresane/main.py:365-457 (one host round trip per iteration). One call
+ * runs a whole minor loop on the device: x = 0, model sources = 0,
+ * r = p = rec, then CG iterations until one of the reference's stop rules
+ * fires (main.py:420-455) or minor_loop_miter iterations are done. On
+ * return x holds the solution the reference keeps (its xn when the loop
+ * converged or hit the iteration cap, the previous x otherwise).
+ * --------------------------------------------------------------------------- */
+#define MSN_MINOR_RUNNING 0
+#define MSN_MINOR_FALSE_DETECTION 1 /* minor == 1 and SNR > 40: xn discarded */
+#define MSN_MINOR_CONVERGED 2       /* SNR > 40: xn kept */
+#define MSN_MINOR_STALLED 3         /* minor > 2 and SNR <= previous SNR: xn discarded */
+#define MSN_MINOR_ITERATION_CAP 4   /* minor == minor_loop_miter: xn kept */
+
+typedef struct msn_minor_args {
+    int n;                  /* sub-region side: every vector is n x n, row-major */
+    int m;                  /* FFT grid side of spec (2n linear, n circular) */
+    int linear;             /* convolution mode of msn_fft_convolve */
+    int max_scale;          /* decomposition depth of A */
+    int scale_adjust;       /* first kept scale; planes = max_scale - scale_adjust */
+    int minor_loop_miter;   /* iteration cap */
+    int enforce_positivity; /* clamp xn >= 0 (main.py:392-398) */
+    int reserved;
+    const void *spec;       /* packed sub-PSF spectrum (msn_psf_spectrum) */
+    const float *rec;       /* R(extracted sources): initial r and p */
+    float *x, *xn, *r, *rn, *p, *ap, *tmp; /* n*n each */
+    float *planes;          /* planes x n x n: mask * W(H p) */
+    const float *emask;     /* planes x n x n extraction mask */
+    const float *esrc;      /* planes x n x n extracted sources */
+    float *ms;              /* planes x n x n running model sources */
+    double *scal;           /* 5 doubles: r.r, p.Ap, alpha, rn.rn, beta */
+    double *snr2;           /* 2 doubles: |esrc|^2, |esrc - ms|^2 */
+    int *neg;               /* 1 int: #(xn < 0) */
+    void *fft_work;         /* msn_fft_workspace_bytes(n, m) */
+    size_t fft_work_bytes;
+    void *iuwt_work;        /* msn_iuwt_workspace_bytes(n, n) */
+    size_t iuwt_work_bytes;
+    void *red_work;         /* msn_reduce_workspace_bytes() */
+    size_t red_work_bytes;
+} msn_minor_args;
+
+typedef struct msn_minor_result {
+    int minor;           /* iterations performed */
+    int outcome;         /* MSN_MINOR_* */
+    int positivity_runs; /* iterations that clamped xn */
+    int reserved;
+    double snr_current;  /* SNR of the last iteration */
+    double snr_last;     /* SNR of the iteration before it */
+} msn_minor_result;
+
+/* An engine owns a small device state block, capture streams and the cache of
+ * instantiated graphs (keyed by the whole argument block); it belongs to the
+ * device current at creation. One engine serves one caller thread at a time
+ * (calls are serialised by a lock); use one engine per concurrent
+ * deconvolution. */
+int msn_minor_engine_create(void **engine);
+int msn_minor_engine_destroy(void *engine);
+
+/* Runs one minor loop on stream and waits for it. snr_history (host, may be
+ * NULL) receives the SNR of each iteration, up to history_len entries. */
+int msn_minor_loop(void *engine, const msn_minor_args *args, msn_minor_result *result, double *snr_history,
+                   int history_len, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -59,7 +59,29 @@ SIGNATURES = {
     "msn_sub": (c_int, [c_void_p, c_void_p, c_void_p, c_size_t, c_void_p]),
     "msn_mul": (c_int, [c_void_p, c_void_p, c_void_p, c_size_t, c_void_p]),
     "msn_region_std": (c_int, [c_void_p, c_int, c_int, c_int, c_int, c_int, c_void_p, c_void_p, c_size_t, c_void_p]),
+    "msn_minor_engine_create": (c_int, [ctypes.POINTER(c_void_p)]),
+    "msn_minor_engine_destroy": (c_int, [c_void_p]),
+    "msn_minor_loop": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_void_p]),
 }
+
+MINOR_RUNNING, MINOR_FALSE_DETECTION, MINOR_CONVERGED, MINOR_STALLED, MINOR_ITERATION_CAP = range(5)
+
+
+class MinorArgs(ctypes.Structure):
+    """msn_minor_args of include/msn.h."""
+    _fields_ = [("n", c_int), ("m", c_int), ("linear", c_int), ("max_scale", c_int), ("scale_adjust", c_int),
+                ("minor_loop_miter", c_int), ("enforce_positivity", c_int), ("reserved", c_int),
+                ("spec", c_void_p), ("rec", c_void_p), ("x", c_void_p), ("xn", c_void_p), ("r", c_void_p),
+                ("rn", c_void_p), ("p", c_void_p), ("ap", c_void_p), ("tmp", c_void_p), ("planes", c_void_p),
+                ("emask", c_void_p), ("esrc", c_void_p), ("ms", c_void_p), ("scal", c_void_p), ("snr2", c_void_p),
+                ("neg", c_void_p), ("fft_work", c_void_p), ("fft_work_bytes", c_size_t), ("iuwt_work", c_void_p),
+                ("iuwt_work_bytes", c_size_t), ("red_work", c_void_p), ("red_work_bytes", c_size_t)]
+
+
+class MinorResult(ctypes.Structure):
+    """msn_minor_result of include/msn.h."""
+    _fields_ = [("minor", c_int), ("outcome", c_int), ("positivity_runs", c_int), ("reserved", c_int),
+                ("snr_current", c_double), ("snr_last", c_double)]
 
 
 class MsnError(RuntimeError):

@@ -27,7 +27,20 @@ int check_cuda(cudaError_t e, const char *what) {
 
 static std::atomic<unsigned long long> g_launches{0};
 
-void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+static thread_local unsigned long long t_launches = 0;
+
+void count_launch() {
+    g_launches.fetch_add(1, std::memory_order_relaxed);
+    ++t_launches;
+}
+
+// Launches issued by the calling thread (graph capture measures its own).
+unsigned long long thread_launches() { return t_launches; }
+
+// Graph executions: captured launches are taken out, executed ones added.
+void adjust_launches(long long delta) {
+    g_launches.fetch_add((unsigned long long)delta, std::memory_order_relaxed);
+}
 
 }  // namespace msn
 

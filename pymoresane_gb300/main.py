@@ -13,6 +13,7 @@ Signatures and defaults follow the reference except that the mode arguments
 default to the GPU path ('gpu'); CPU modes raise ValueError (this package
 has no CPU implementation). See INTEGRATION.md for every difference.
 """
+import ctypes
 import logging
 import math
 
@@ -103,6 +104,11 @@ class Deconvolver:
         # linearity) instead of recomputing mask * W(H xn) with a convolution and a
         # decomposition every minor iteration as pymoresane/main.py:413-416 does.
         self.incremental_snr = True
+        # True: each minor loop runs as one CUDA graph with its stop rules on the
+        # device (msn_minor_loop); False: the host drives every iteration, as the
+        # reference does (pymoresane/main.py:365-457).
+        self.native_minor_loop = True
+        self._engine = None
         self._psf_cache = _PsfCache()
         self._bufs = {}
 
@@ -166,6 +172,39 @@ class Deconvolver:
             self._bufs = {key: _Buffers(ns, self.dirty_data_shape[0], spec_sub.m, spec_data.m, scale_count,
                                         self.device)}
         return self._bufs[key]
+
+    def _native_minor(self, B, V, spec_sub, linear, max_scale, scale_adjust, planes, ns, miter, positivity, st):
+        """One minor loop through msn_minor_loop; returns (MinorResult, per-iteration SNRs)."""
+        if self._engine is None:
+            h = ctypes.c_void_p()
+            _native.call("msn_minor_engine_create", ctypes.byref(h))
+            self._engine = h
+        a = _native.MinorArgs()
+        a.n, a.m, a.linear = ns, spec_sub.m, 1 if linear else 0
+        a.max_scale, a.scale_adjust = max_scale, scale_adjust
+        a.minor_loop_miter, a.enforce_positivity = int(miter), 1 if positivity else 0
+        a.spec = spec_sub.packed.data_ptr()
+        a.rec = V["rec"].data_ptr()
+        for name in ("x", "xn", "r", "rn", "p", "ap", "tmp"):
+            setattr(a, name, V[name].data_ptr())
+        a.planes, a.emask, a.esrc, a.ms = (B.planes.data_ptr(), B.emask.data_ptr(), B.esrc.data_ptr(),
+                                           B.ms.data_ptr())
+        a.scal, a.snr2, a.neg = B.scal.data_ptr(), B.snr2.data_ptr(), B.neg.data_ptr()
+        a.fft_work, a.fft_work_bytes = B.fft_work.data_ptr(), B.fft_work.numel()
+        a.iuwt_work, a.iuwt_work_bytes = B.iuwt_work.data_ptr(), B.iuwt_work.numel()
+        a.red_work, a.red_work_bytes = B.red_work.data_ptr(), B.red_work.numel()
+        res = _native.MinorResult()
+        hist = (ctypes.c_double * max(int(miter), 1))()
+        _native.call("msn_minor_loop", self._engine, ctypes.byref(a), ctypes.byref(res), hist, len(hist), st)
+        return res, list(hist[:min(res.minor, len(hist))])
+
+    def __del__(self):
+        eng, self._engine = getattr(self, "_engine", None), None
+        if eng is not None:
+            try:
+                _native.query("msn_minor_engine_destroy", eng)
+            except Exception:
+                pass
 
     def moresane(self, dirty, subregion=None, scale_count=None, sigma_level=4, loop_gain=0.1, tolerance=0.75,
                  accuracy=1e-6, major_loop_miter=100, minor_loop_miter=30, conv_mode='linear',
@@ -279,66 +318,82 @@ class Deconvolver:
                                       work=B.tool_work)
                 dev.iuwt_recompose(B.esrc[:planes], scale_adjust, out=V["rec"], work=B.iuwt_work)
 
-                x, xn, r, rn, p, ap = V["x"], V["xn"], V["r"], V["rn"], V["p"], V["ap"]
-                x.zero_()
-                if self.incremental_snr:
-                    B.ms[:planes].zero_()
-                r.copy_(V["rec"])
-                p.copy_(V["rec"])
-                minor = 0
-                snr_last = snr_current = 0.0
-                while minor < minor_loop_miter:
-                    apply_a(p, ap, max_scale, scale_adjust, planes)
-                    dev.dot2(r.reshape(-1), r.reshape(-1), p.reshape(-1), ap.reshape(-1), out=B.scal[0:2],
-                             work=B.red_work)
-                    call("msn_cg_alpha_x", x.data_ptr(), p.data_ptr(), B.scal.data_ptr(), xn.data_ptr(), nvec,
-                         B.neg.data_ptr(), st)
-                    if enforce_positivity and int(B.neg.item()) > 0:
-                        call("msn_cg_positivity", x.data_ptr(), xn.data_ptr(), p.data_ptr(), B.scal.data_ptr(),
-                             nvec, st)
-                        apply_a(p, ap, max_scale, scale_adjust, planes)
-                    call("msn_cg_residual", r.data_ptr(), ap.data_ptr(), B.scal.data_ptr(), rn.data_ptr(), nvec,
-                         B.red_work.data_ptr(), B.red_work.numel(), st)
-                    call("msn_cg_direction", rn.data_ptr(), p.data_ptr(), B.scal.data_ptr(), nvec, st)
-                    # model_sources = mask * W(H xn) and the SNR against the extracted sources
-                    if self.incremental_snr:
-                        # ms += alpha * (mask * W(H p)), the plane stack left in B.planes by apply_a
-                        call("msn_snr_update", B.esrc.data_ptr(), B.ms.data_ptr(), B.planes.data_ptr(),
-                             B.scal.data_ptr(), planes * nvec, B.snr2.data_ptr(), B.red_work.data_ptr(),
-                             B.red_work.numel(), st)
-                    else:
-                        dev.fft_convolve(xn, spec_sub, linear, out=V["tmp"], work=B.fft_work)
-                        w = B.planes[:planes]
-                        dev.iuwt_decompose_masked(V["tmp"], B.emask, max_scale, scale_adjust, out=w,
-                                                  work=B.iuwt_work)
-                        dev.snr_sums(B.esrc[:planes].reshape(-1), w.reshape(-1), out=B.snr2, work=B.red_work)
-                    s2 = B.snr2.cpu().numpy()
-                    snr_last = snr_current
-                    with np.errstate(divide="ignore", invalid="ignore"):
-                        snr_current = float(20 * np.log10(np.sqrt(s2[0]) / np.sqrt(s2[1])))
-                    minor += 1
-                    logger.debug("SNR at iteration %d = %s", minor, snr_current)
-                    if minor == 1 and snr_current > 40:
+                if self.native_minor_loop:
+                    res, hist = self._native_minor(B, V, spec_sub, linear, max_scale, scale_adjust, planes, ns,
+                                                   minor_loop_miter, enforce_positivity, st)
+                    minor, snr_current = res.minor, res.snr_current
+                    for i, v in enumerate(hist):
+                        logger.debug("SNR at iteration %d = %s", i + 1, v)
+                    if res.outcome == _native.MINOR_FALSE_DETECTION:
                         logger.info("SNR too large on first iteration - false detection. "
                                     "Incrementing the minimum scale.")
                         min_scale += 1
-                        break
-                    if snr_current > 40:
+                    elif res.outcome == _native.MINOR_CONVERGED:
                         logger.info("Model has reached <1% error - exiting minor loop.")
+                        min_scale = 0
+                    elif res.outcome == _native.MINOR_STALLED:
+                        min_scale = 0 if snr_current > 10.5 else min_scale + 1
+                else:
+                    x, xn, r, rn, p, ap = V["x"], V["xn"], V["r"], V["rn"], V["p"], V["ap"]
+                    x.zero_()
+                    if self.incremental_snr:
+                        B.ms[:planes].zero_()
+                    r.copy_(V["rec"])
+                    p.copy_(V["rec"])
+                    minor = 0
+                    snr_last = snr_current = 0.0
+                    while minor < minor_loop_miter:
+                        apply_a(p, ap, max_scale, scale_adjust, planes)
+                        dev.dot2(r.reshape(-1), r.reshape(-1), p.reshape(-1), ap.reshape(-1), out=B.scal[0:2],
+                                 work=B.red_work)
+                        call("msn_cg_alpha_x", x.data_ptr(), p.data_ptr(), B.scal.data_ptr(), xn.data_ptr(), nvec,
+                             B.neg.data_ptr(), st)
+                        if enforce_positivity and int(B.neg.item()) > 0:
+                            call("msn_cg_positivity", x.data_ptr(), xn.data_ptr(), p.data_ptr(), B.scal.data_ptr(),
+                                 nvec, st)
+                            apply_a(p, ap, max_scale, scale_adjust, planes)
+                        call("msn_cg_residual", r.data_ptr(), ap.data_ptr(), B.scal.data_ptr(), rn.data_ptr(), nvec,
+                             B.red_work.data_ptr(), B.red_work.numel(), st)
+                        call("msn_cg_direction", rn.data_ptr(), p.data_ptr(), B.scal.data_ptr(), nvec, st)
+                        # model_sources = mask * W(H xn) and the SNR against the extracted sources
+                        if self.incremental_snr:
+                            # ms += alpha * (mask * W(H p)), the plane stack left in B.planes by apply_a
+                            call("msn_snr_update", B.esrc.data_ptr(), B.ms.data_ptr(), B.planes.data_ptr(),
+                                 B.scal.data_ptr(), planes * nvec, B.snr2.data_ptr(), B.red_work.data_ptr(),
+                                 B.red_work.numel(), st)
+                        else:
+                            dev.fft_convolve(xn, spec_sub, linear, out=V["tmp"], work=B.fft_work)
+                            w = B.planes[:planes]
+                            dev.iuwt_decompose_masked(V["tmp"], B.emask, max_scale, scale_adjust, out=w,
+                                                      work=B.iuwt_work)
+                            dev.snr_sums(B.esrc[:planes].reshape(-1), w.reshape(-1), out=B.snr2, work=B.red_work)
+                        s2 = B.snr2.cpu().numpy()
+                        snr_last = snr_current
+                        with np.errstate(divide="ignore", invalid="ignore"):
+                            snr_current = float(20 * np.log10(np.sqrt(s2[0]) / np.sqrt(s2[1])))
+                        minor += 1
+                        logger.debug("SNR at iteration %d = %s", minor, snr_current)
+                        if minor == 1 and snr_current > 40:
+                            logger.info("SNR too large on first iteration - false detection. "
+                                        "Incrementing the minimum scale.")
+                            min_scale += 1
+                            break
+                        if snr_current > 40:
+                            logger.info("Model has reached <1% error - exiting minor loop.")
+                            V["x"], V["xn"] = xn, x
+                            x, xn = xn, x
+                            min_scale = 0
+                            break
+                        if minor > 2 and snr_current <= snr_last:
+                            if snr_current > 10.5:
+                                min_scale = 0
+                            else:
+                                min_scale += 1
+                            break
+                        V["r"], V["rn"] = rn, r
+                        r, rn = rn, r
                         V["x"], V["xn"] = xn, x
                         x, xn = xn, x
-                        min_scale = 0
-                        break
-                    if minor > 2 and snr_current <= snr_last:
-                        if snr_current > 10.5:
-                            min_scale = 0
-                        else:
-                            min_scale += 1
-                        break
-                    V["r"], V["rn"] = rn, r
-                    r, rn = rn, r
-                    V["x"], V["xn"] = xn, x
-                    x, xn = xn, x
                 have_x = True
                 logger.info("%d minor loop iterations performed.", minor)
                 rec.update(max_scale=max_scale, scale_adjust=scale_adjust, minor=minor, snr=snr_current)

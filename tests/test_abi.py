@@ -49,3 +49,28 @@ def test_host_queries(lib):
     assert _native.query("msn_iuwt_workspace_bytes", 64, 64) == 2 * 64 * 64 * 4
     assert _native.query("msn_iuwt_workspace_bytes", 0, 64) == 0
     assert _native.query("msn_last_error") == b""
+
+
+def test_minor_structs_match_header(tmp_path):
+    """The ctypes mirrors of msn_minor_args / msn_minor_result have the C layout (gcc on the header)."""
+    import shutil
+    import subprocess
+    if shutil.which("gcc") is None:
+        pytest.skip("gcc not available")
+    structs = {"msn_minor_args": _native.MinorArgs, "msn_minor_result": _native.MinorResult}
+    lines = ["#include <stdio.h>", "#include <stddef.h>", '#include "msn.h"', "int main(void) {"]
+    for cname, cls in structs.items():
+        lines.append(f'printf("{cname} size %zu\\n", sizeof({cname}));')
+        for f, _ in cls._fields_:
+            lines.append(f'printf("{cname} {f} %zu\\n", offsetof({cname}, {f}));')
+    lines += ["return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split("\n")
+    for line in filter(None, out):
+        cname, field, value = line.split()
+        cls = structs[cname]
+        got = ctypes.sizeof(cls) if field == "size" else getattr(cls, field).offset
+        assert got == int(value), (cname, field, got, value)

@@ -109,10 +109,35 @@ def test_incremental_model_sources_same_decisions(cuda, name):
     runs = []
     for inc in (True, False):
         eng = Deconvolver(g[f"{name}_psf"])
+        eng.native_minor_loop = False
         eng.incremental_snr = inc
         model, residual, major = eng.moresane(dirty, **kw)
         runs.append((eng.log, model.cpu().numpy()))
     (la, ma), (lb, mb) = runs
+    assert [(r["max_scale"], r["scale_adjust"], r["minor"]) for r in la] == \
+           [(r["max_scale"], r["scale_adjust"], r["minor"]) for r in lb]
+    assert np.max(np.abs(ma - mb)) <= MODEL_TOL * np.max(np.abs(mb))
+
+
+@pytest.mark.parametrize("name", ["lin_double", "circ_pos", "neg_excl"])
+def test_native_minor_loop_matches_host_loop(cuda, name):
+    # One CUDA graph per minor loop with the stop rules on the device against the
+    # host-driven loop over the same kernels: same decisions, same iteration counts,
+    # same model.
+    from pymoresane_gb300.main import Deconvolver
+    import torch
+    g = np.load(os.path.join(GOLDEN, "moresane.npz"))
+    pk, rk = mg.MORESANE_CASES[name]
+    kw = dict(mg.RUN_DEFAULTS, **rk)
+    dirty = torch.from_numpy(g[f"{name}_dirty"]).cuda()
+    runs = []
+    for native in (True, False):
+        eng = Deconvolver(g[f"{name}_psf"])
+        eng.native_minor_loop = native
+        model, residual, major = eng.moresane(dirty, **kw)
+        runs.append((eng.log, model.cpu().numpy(), major))
+    (la, ma, ka), (lb, mb, kb) = runs
+    assert ka == kb
     assert [(r["max_scale"], r["scale_adjust"], r["minor"]) for r in la] == \
            [(r["max_scale"], r["scale_adjust"], r["minor"]) for r in lb]
     assert np.max(np.abs(ma - mb)) <= MODEL_TOL * np.max(np.abs(mb))
