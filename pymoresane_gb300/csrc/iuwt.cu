@@ -1,12 +1,12 @@
 // Isotropic undecimated wavelet transform (a trous, B3 spline) for sm_103a.
 //
 // One kernel launch performs one complete separable smoothing at dilation d:
-// a CTA owns J full-width rows of one residue class (rows k, k + d, k + 2d, ...
-// of the image); the axis-0 (vertical) pass slides its five taps along that
-// class, so J output rows cost J + 4 float4 row loads, and leaves the J rows in
-// shared memory; the axis-1 (horizontal) pass then runs entirely out of shared
-// memory, so any dilation up to the row length is handled without a horizontal
-// halo. The epilogue optionally fuses the
+// a CTA owns a band of full-width rows; the axis-0 (vertical) pass reads the
+// five taps straight from global memory with float4 loads (the taps of one
+// output row are whole rows r, r +- d, r +- 2d, mirrored at the borders) and
+// leaves the band in shared memory; the axis-1 (horizontal) pass then runs
+// entirely out of shared memory, so any dilation up to the row length is
+// handled without a horizontal halo. The epilogue optionally fuses the
 // wavelet detail (w = C_s - smooth(C_{s+1})) or the recomposition add
 // (rec = smooth(rec) + w), so no separate elementwise pass is ever launched.
 //
@@ -83,57 +83,46 @@ __device__ __forceinline__ float4 horizontal4(const float *__restrict__ s, int c
     return v;
 }
 
-// One smoothing pass at dilation d over the output rows r = k + j d,
-// j0 <= j < j0 + J, of one residue class k (mod d). Along a class the vertical
-// taps of consecutive outputs are consecutive class rows, so the J outputs need
-// only J + 4 input rows (each fetched once, all of them in flight together)
-// instead of 5 J; the mirror at the borders is applied to the row index, so the
-// sliding window stays exact there too. The J vertical results stay in shared
-// memory as full rows, and the horizontal pass plus the epilogue run from there.
-template <int EPI, int J>
+template <int EPI>
 __global__ void __launch_bounds__(kThreads)
-atrous_class(const float *__restrict__ in, float *__restrict__ out, const float *__restrict__ aux,
-             const float *__restrict__ mask, int ny, int nx, int d) {
+atrous_band(const float *__restrict__ in, float *__restrict__ out, const float *__restrict__ aux,
+            const float *__restrict__ mask, int ny, int nx, int d, int band_rows) {
     extern __shared__ float4 smem4[];
     const float *band = reinterpret_cast<const float *>(smem4);
-    const int k = (int)(blockIdx.x % (unsigned)d);
-    const int j0 = (int)(blockIdx.x / (unsigned)d) * J;
-    const int r0 = k + j0 * d;
-    if (r0 >= ny) return;
-    const int class_rows = (ny - 1 - k) / d + 1;
-    const int rows = min(J, class_rows - j0);
+    const int r0 = blockIdx.x * band_rows;
+    const int rows = min(band_rows, ny - r0);
     const int nx4 = nx >> 2;
+    const int total4 = rows * nx4;
     const float4 *in4 = reinterpret_cast<const float4 *>(in);
 
-    // Axis 0: J + 4 row loads per float4 column, issued together, then J taps.
-    for (int c4 = threadIdx.x; c4 < nx4; c4 += blockDim.x) {
-        float4 t[J + 4];
-#pragma unroll
-        for (int m = 0; m < J + 4; ++m) {
-            if (m < rows + 4) {
-                const int r = mirror(r0 + (m - 2) * d, ny);
-                t[m] = __ldg(in4 + (size_t)r * nx4 + c4);
-            } else {
-                t[m] = make_float4(0.f, 0.f, 0.f, 0.f);
-            }
-        }
-#pragma unroll
-        for (int m = 0; m < J; ++m)
-            if (m < rows) smem4[m * nx4 + c4] = b3_tap4(t[m + 2], t[m], t[m + 1], t[m + 3], t[m + 4]);
+    // Axis 0: two float4 columns per thread per iteration keep ten loads in flight.
+    const int nt = blockDim.x;
+    int i = threadIdx.x;
+    for (; i + nt < total4; i += 2 * nt) {
+        const int i2 = i + nt;
+        const int rr1 = i / nx4, rr2 = i2 / nx4;
+        const Taps4 t1 = load_vertical(in4, r0 + rr1, i - rr1 * nx4, ny, nx4, d);
+        const Taps4 t2 = load_vertical(in4, r0 + rr2, i2 - rr2 * nx4, ny, nx4, d);
+        smem4[i] = b3_tap4(t1.c, t1.a, t1.b, t1.e, t1.f);
+        smem4[i2] = b3_tap4(t2.c, t2.a, t2.b, t2.e, t2.f);
+    }
+    if (i < total4) {
+        const int rr = i / nx4;
+        const Taps4 t = load_vertical(in4, r0 + rr, i - rr * nx4, ny, nx4, d);
+        smem4[i] = b3_tap4(t.c, t.a, t.b, t.e, t.f);
     }
     __syncthreads();
 
     // Axis 1 out of shared memory (four columns per thread), fused epilogue, float4 stores.
     const float4 *aux4 = reinterpret_cast<const float4 *>(aux);
     float4 *out4 = reinterpret_cast<float4 *>(out);
-    const int total4 = rows * nx4;
-    for (int i = threadIdx.x; i < total4; i += blockDim.x) {
-        const int m = i / nx4;
-        const int c4 = i - m * nx4;
-        const size_t g4 = (size_t)(r0 + m * d) * nx4 + c4;
+    for (int j = threadIdx.x; j < total4; j += nt) {
+        const int rr = j / nx4;
+        const int c4 = j - rr * nx4;
+        const size_t g4 = (size_t)(r0 + rr) * nx4 + c4;
         float4 x;
         if (EPI != kStore) x = __ldg(aux4 + g4);
-        float4 v = horizontal4(band + m * nx, c4 * 4, nx, d);
+        float4 v = horizontal4(band + rr * nx, c4 * 4, nx, d);
         if (EPI == kDetail || EPI == kDetailMask) {
             v.x = __fsub_rn(x.x, v.x);
             v.y = __fsub_rn(x.y, v.y);
@@ -141,11 +130,11 @@ atrous_class(const float *__restrict__ in, float *__restrict__ out, const float 
             v.w = __fsub_rn(x.w, v.w);
         }
         if (EPI == kDetailMask) {  // mask * detail, as the reference's separate product (main.py:383)
-            const float4 mk = __ldg(reinterpret_cast<const float4 *>(mask) + g4);
-            v.x = __fmul_rn(v.x, mk.x);
-            v.y = __fmul_rn(v.y, mk.y);
-            v.z = __fmul_rn(v.z, mk.z);
-            v.w = __fmul_rn(v.w, mk.w);
+            const float4 m = __ldg(reinterpret_cast<const float4 *>(mask) + g4);
+            v.x = __fmul_rn(v.x, m.x);
+            v.y = __fmul_rn(v.y, m.y);
+            v.z = __fmul_rn(v.z, m.z);
+            v.w = __fmul_rn(v.w, m.w);
         }
         if (EPI == kAdd) {
             v.x = __fadd_rn(v.x, x.x);
@@ -171,39 +160,27 @@ __global__ void zero_plus(const float4 *__restrict__ w, float4 *__restrict__ out
     }
 }
 
-// Rows per CTA: the largest J in {8, 4, 2, 1} whose shared band stays within
-// 64 KB (three or more CTAs per SM) and that still gives one CTA per SM.
-int class_rows_for(int ny, int nx) {
-    int j = 8;
-    while (j > 1 && ((size_t)j * nx * sizeof(float) > 64 * 1024 || (ny + j - 1) / j < 152)) j >>= 1;
-    return j;
-}
-
-template <int EPI, int J>
-int launch_class(const float *in, float *out, const float *aux, const float *mask, int ny, int nx, int d,
-                 cudaStream_t st) {
-    static std::once_flag once;
-    std::call_once(once, [] {
-        cudaFuncSetAttribute(atrous_class<EPI, J>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxSmem);
-    });
-    const size_t smem = (size_t)J * nx * sizeof(float);
-    const int per_class = (ny + d - 1) / d;
-    const int grid = d * ((per_class + J - 1) / J);
-    const int nx4 = nx >> 2;
-    const int threads = nx4 >= kThreads ? kThreads : ((nx4 + 31) / 32) * 32;
-    atrous_class<EPI, J><<<grid, threads, smem, st>>>(in, out, aux, mask, ny, nx, d);
-    return check_launch("atrous_class");
-}
+// One row per CTA. Measured on GB300 (one smoothing pass, d = 1 .. 256):
+// 2048^2 10.3-14.4 us and 4096^2 33.9-45.1 us with one row, against 12.4-16.4
+// and 43.0-63.5 us with three; a plain float4 copy of the same plane takes
+// 6.2 and 22.6 us. Rows of the same dilation class that share vertical taps
+// are then neighbouring CTAs, which read them from L2 close together in time.
+int band_rows_for(int, int) { return 1; }
 
 template <int EPI>
 int launch_band(const float *in, float *out, const float *aux, int ny, int nx, int d, cudaStream_t st,
                 const float *mask = nullptr) {
-    switch (class_rows_for(ny, nx)) {
-        case 8: return launch_class<EPI, 8>(in, out, aux, mask, ny, nx, d, st);
-        case 4: return launch_class<EPI, 4>(in, out, aux, mask, ny, nx, d, st);
-        case 2: return launch_class<EPI, 2>(in, out, aux, mask, ny, nx, d, st);
-        default: return launch_class<EPI, 1>(in, out, aux, mask, ny, nx, d, st);
-    }
+    static std::once_flag once;
+    std::call_once(once, [] {
+        cudaFuncSetAttribute(atrous_band<EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxSmem);
+    });
+    const int band = band_rows_for(ny, nx);
+    const size_t smem = (size_t)band * nx * sizeof(float);
+    const int grid = (ny + band - 1) / band;
+    const int work4 = band * (nx >> 2);
+    const int threads = work4 >= kThreads ? kThreads : ((work4 + 31) / 32) * 32;
+    atrous_band<EPI><<<grid, threads, smem, st>>>(in, out, aux, mask, ny, nx, d, band);
+    return check_launch("atrous_band");
 }
 
 int launch_zero_plus(const float *w, float *out, size_t n, cudaStream_t st) {
