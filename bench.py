@@ -313,6 +313,100 @@ def run_deconv(args, rank, world, dist):
             "dirty": dirty_h, "psf": psf_h, "model_sum": float(img.model.sum()), "e2e_steps": e2e_steps}
 
 
+# ---------------------------------------------------------------------------
+# Batched (64 mixed-size images) and served (Poisson arrivals) workloads
+# ---------------------------------------------------------------------------
+
+BATCH_SIZES, BATCH_P = (256, 512, 1024, 1536, 2048), (0.2, 0.3, 0.25, 0.15, 0.1)
+SERVE_SIZES, SERVE_P = (512, 1024, 1536, 2048, 4096), (0.35, 0.3, 0.15, 0.15, 0.05)
+MIX_KW = dict(sigma_level=4, loop_gain=0.2, tolerance=0.75, accuracy=1e-6, major_loop_miter=100,
+              minor_loop_miter=30, conv_mode="linear")
+
+
+def mix_job(n, seed):
+    """Config-0 style problem scaled by area to side n (PSF 2n, uv count and sources ~ n^2), S = log2(n) - 3."""
+    from pymoresane_gb300 import synthetic
+    from pymoresane_gb300.batch import Job
+    dirty, psf, _ = synthetic.make_problem(synthetic.scaled(n, seed=seed))
+    return Job(dirty, psf, kwargs=dict(MIX_KW, scale_count=int(np.log2(n)) - 3), tag=(n, seed))
+
+
+def run_plain(jobs):
+    """The jobs one at a time through the plain single-image path; (seconds, latencies in ms from t=0)."""
+    import torch
+
+    from pymoresane_gb300.main import Deconvolver
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    lat, models = [], []
+    for j in jobs:
+        t1 = time.perf_counter()
+        eng = Deconvolver(j.psf)
+        model, residual, _ = eng.moresane(torch.from_numpy(j.dirty).cuda(), **j.kwargs)
+        models.append(model.cpu().numpy())
+        residual.cpu()
+        lat.append((time.perf_counter() - t1) * 1e3)
+    return time.perf_counter() - t0, lat, models
+
+
+def run_batch(args, rank):
+    """64 images of sizes {256..2048} (p = .2 .3 .25 .15 .1), batched vs one at a time."""
+    from pymoresane_gb300.batch import DeconvolutionExecutor
+    rng = np.random.default_rng(1000 + rank)
+    sizes = rng.choice(BATCH_SIZES, size=args.images, p=BATCH_P)
+    cache = {}
+    jobs = []
+    for i, n in enumerate(sizes):
+        key = (int(n), i % args.distinct)
+        if key not in cache:
+            cache[key] = mix_job(int(n), seed=2000 + 97 * key[1] + int(n))
+        jobs.append(cache[key])
+    # warm-up: one job per size through both paths (allocator pools, PSF plans, graph capture code)
+    warm = [cache[k] for k in sorted({(k[0], 0) for k in cache})]
+    run_plain(warm)
+    with DeconvolutionExecutor(workers=args.workers, order="largest") as ex:
+        ex.map(warm)
+    plain_s, plain_lat, plain_models = run_plain(jobs)
+    with DeconvolutionExecutor(workers=args.workers, order="largest") as ex:
+        t0 = time.perf_counter()
+        res = ex.map(jobs)
+        batch_s = time.perf_counter() - t0
+    lat = [r.latency * 1e3 for r in res]
+    same = all(np.array_equal(m, r.model) for m, r in zip(plain_models, res))
+    return {"images": len(jobs), "plain_s": plain_s, "batch_s": batch_s, "lat": lat, "plain_lat": plain_lat,
+            "sizes": {int(n): int((sizes == n).sum()) for n in BATCH_SIZES}, "same": same}
+
+
+def run_serve(args, rank):
+    """Poisson arrivals (lambda = 40/s) of sizes {512..4096} (p = .35 .3 .15 .15 .05), served vs one at a time."""
+    from pymoresane_gb300.batch import serve
+    rng = np.random.default_rng(3000 + rank)
+    sizes = rng.choice(SERVE_SIZES, size=args.requests, p=SERVE_P)
+    arrivals = np.cumsum(rng.exponential(1.0 / args.rate, size=args.requests))
+    cache = {}
+    jobs = []
+    for i, n in enumerate(sizes):
+        key = (int(n), i % args.distinct)
+        if key not in cache:
+            cache[key] = mix_job(int(n), seed=4000 + 97 * key[1] + int(n))
+        jobs.append(cache[key])
+    warm = [cache[k] for k in sorted({(k[0], 0) for k in cache})]
+    run_plain(warm)
+    serve(warm, [0.0] * len(warm), workers=args.workers)
+    plain_s, plain_lat, plain_models = run_plain(jobs)
+    res, wall = serve(jobs, list(arrivals), workers=args.workers)
+    lat = [r.latency * 1e3 for r in res]
+    same = all(np.array_equal(m, r.model) for m, r in zip(plain_models, res))
+    # the same jobs one at a time, arriving at the same times (queueing included)
+    t_free, seq_lat = 0.0, []
+    for at, pl in zip(arrivals, plain_lat):
+        start = max(at, t_free)
+        t_free = start + pl / 1e3
+        seq_lat.append((t_free - at) * 1e3)
+    return {"requests": len(jobs), "wall_s": wall, "plain_s": plain_s, "lat": lat, "seq_lat": seq_lat, "same": same,
+            "arrival_span_s": float(arrivals[-1]), "sizes": {int(n): int((sizes == n).sum()) for n in SERVE_SIZES}}
+
+
 def conv_roofline(n=2048, m=4096, reps=50):
     """Average duration of the fused linear convolution (the minor loop's dominant step) at 2048^2 / 4096^2.
 
@@ -356,7 +450,12 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="deconv", choices=["deconv", "iuwt", "conv"])
+    ap.add_argument("--workload", default="deconv", choices=["deconv", "iuwt", "conv", "batch", "serve"])
+    ap.add_argument("--workers", type=int, default=8, help="concurrent streams (batch / serve / served deconv)")
+    ap.add_argument("--images", type=int, default=64, help="batch workload: images")
+    ap.add_argument("--requests", type=int, default=100, help="serve workload: requests")
+    ap.add_argument("--rate", type=float, default=40.0, help="serve workload: arrivals per second")
+    ap.add_argument("--distinct", type=int, default=3, help="batch / serve: distinct problems per size")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
@@ -414,6 +513,39 @@ def main():
                               "value": alg / (us * 1e-6) / 1e9, "unit": "GB/s", "n_gpus": world, "steps": args.steps,
                               "warmup": args.warmup, "us_per_conv": us, "algorithmic_bytes": alg,
                               "frac_of_hbm": alg / (us * 1e-6) / 1e9 / hbm_peak}))
+        return
+
+    if args.workload in ("batch", "serve"):
+        sampler = ClockSampler(gpu_uuid()) if rank == 0 else None
+        if sampler:
+            sampler.start()
+        r = run_batch(args, rank) if args.workload == "batch" else run_serve(args, rank)
+        clocks = sampler.stop() if sampler else None
+        if rank == 0:
+            n_img = r["images"] if args.workload == "batch" else r["requests"]
+            mixed_s = r["batch_s"] if args.workload == "batch" else r["wall_s"]
+            line = {
+                "metric": ("64-image mixed-size batch, images/s (batched vs one at a time)" if args.workload == "batch"
+                           else f"served deconvolutions/s under Poisson arrivals (lambda={args.rate:g}/s)"),
+                "value": world * n_img / mixed_s, "unit": "images/s", "n_gpus": world, "steps": 1, "warmup": 1,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                "data": "synthetic",
+                "config": {"workload": args.workload, "workers": args.workers, "sizes": r["sizes"],
+                           "distinct_problems_per_size": args.distinct,
+                           "parallelism": f"{args.workers} streams x {world} replicas"},
+                "plain": {"value": n_img / r["plain_s"], "unit": "images/s", "seconds": r["plain_s"]},
+                "speedup_vs_plain": r["plain_s"] / mixed_s,
+                "latency_ms": {"p50": percentile(r["lat"], 50), "p99": percentile(r["lat"], 99)},
+                "clocks": clocks,
+            }
+            line["same_result_alone_and_in_mix"] = r["same"]
+            if args.workload == "serve":
+                line["plain_latency_ms"] = {"p50": percentile(r["seq_lat"], 50), "p99": percentile(r["seq_lat"], 99),
+                                            "mode": "same arrivals served one at a time"}
+                line["arrival_span_s"] = r["arrival_span_s"]
+            print(json.dumps(line))
+        if dist:
+            dist.destroy_process_group()
         return
 
     if args.workload == "iuwt":

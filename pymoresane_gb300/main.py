@@ -90,7 +90,7 @@ class Deconvolver:
     GPU; DataImage wraps it with the reference's host-array interface.
     """
 
-    def __init__(self, psf, mask=None, dirty_shape=None):
+    def __init__(self, psf, mask=None, dirty_shape=None, workspace=None):
         dev.require_cuda()
         _native.load()
         self.device = torch.device("cuda", torch.cuda.current_device())
@@ -111,6 +111,10 @@ class Deconvolver:
         self._engine = None
         self._psf_cache = _PsfCache()
         self._bufs = {}
+        # A Workspace (pymoresane_gb300.batch) shared by the deconvolutions that one
+        # worker runs one after another: buffers, the sub-PSF spectrum slot and the
+        # minor-loop engine (with its cached graphs) outlive this object.
+        self.workspace = workspace
 
     def _spectra(self, subregion, conv_mode):
         """(spec_sub, spec_data, psf_subregion) per pymoresane/main.py:118-213 (GPU branches)."""
@@ -168,22 +172,31 @@ class Deconvolver:
 
     def _buffers(self, ns, scale_count, spec_sub, spec_data):
         key = (self.dirty_data_shape[0], ns, scale_count, spec_sub.m, spec_data.m)
+        if self.workspace is not None:
+            return self.workspace.buffers_for(key, lambda: _Buffers(ns, self.dirty_data_shape[0], spec_sub.m,
+                                                                    spec_data.m, scale_count, self.device))
         if key not in self._bufs:
             self._bufs = {key: _Buffers(ns, self.dirty_data_shape[0], spec_sub.m, spec_data.m, scale_count,
                                         self.device)}
         return self._bufs[key]
 
-    def _native_minor(self, B, V, spec_sub, linear, max_scale, scale_adjust, planes, ns, miter, positivity, st):
-        """One minor loop through msn_minor_loop; returns (MinorResult, per-iteration SNRs)."""
+    def _engine_handle(self):
+        if self.workspace is not None:
+            return self.workspace.engine()
         if self._engine is None:
             h = ctypes.c_void_p()
             _native.call("msn_minor_engine_create", ctypes.byref(h))
             self._engine = h
+        return self._engine
+
+    def _native_minor(self, B, V, spec_sub, linear, max_scale, scale_adjust, planes, ns, miter, positivity, st):
+        """One minor loop through msn_minor_loop; returns (MinorResult, per-iteration SNRs)."""
+        engine = self._engine_handle()
         a = _native.MinorArgs()
         a.n, a.m, a.linear = ns, spec_sub.m, 1 if linear else 0
         a.max_scale, a.scale_adjust = max_scale, scale_adjust
         a.minor_loop_miter, a.enforce_positivity = int(miter), 1 if positivity else 0
-        a.spec = spec_sub.packed.data_ptr()
+        a.spec = (B.spec_slot if self.workspace is not None else spec_sub.packed).data_ptr()
         a.rec = V["rec"].data_ptr()
         for name in ("x", "xn", "r", "rn", "p", "ap", "tmp"):
             setattr(a, name, V[name].data_ptr())
@@ -195,7 +208,7 @@ class Deconvolver:
         a.red_work, a.red_work_bytes = B.red_work.data_ptr(), B.red_work.numel()
         res = _native.MinorResult()
         hist = (ctypes.c_double * max(int(miter), 1))()
-        _native.call("msn_minor_loop", self._engine, ctypes.byref(a), ctypes.byref(res), hist, len(hist), st)
+        _native.call("msn_minor_loop", engine, ctypes.byref(a), ctypes.byref(res), hist, len(hist), st)
         return res, list(hist[:min(res.minor, len(hist))])
 
     def __del__(self):
@@ -232,6 +245,11 @@ class Deconvolver:
         linear = conv_mode == "linear"
         spec_sub, spec_data, psf_sub = self._spectra(subregion, conv_mode)
         B = self._buffers(ns, scale_count, spec_sub, spec_data)
+        if self.workspace is not None:
+            # a fixed device address for the sub-PSF spectrum keeps the cached minor-loop graphs valid
+            if getattr(B, "spec_slot", None) is None or B.spec_slot.shape != spec_sub.packed.shape:
+                B.spec_slot = torch.empty_like(spec_sub.packed)
+            B.spec_slot.copy_(spec_sub.packed)
         energies = self._energies(psf_sub, scale_count, B)
         st = dev.stream_handle()
         call = _native.call
