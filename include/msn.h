@@ -322,6 +322,96 @@ int msn_minor_engine_destroy(void *engine);
 int msn_minor_loop(void *engine, const msn_minor_args *args, msn_minor_result *result, double *snr_history,
                    int history_len, void *stream);
 
+/* ---------------------------------------------------------------------------
+ * Native MORESANE run (major loop on the host side of the library).
+ *
+ * Replaces the major loop of DataImage.moresane, pymoresane/main.py:266-514,
+ * for one PSF set-up: threshold (MAD, main.py:279-296), scale selection
+ * (main.py:298-335), source extraction (main.py:337-351), the minor loop
+ * (msn_minor_loop), model update, residual and the standard-deviation test
+ * with revert (main.py:466-503). The caller prepares the PSF spectra, the
+ * PSF scale energies and the buffers (sizes below), as the set-up code of
+ * main.py:99-236 does, then one call runs every major iteration with no
+ * interpreter involvement; log events and per-major records are returned in
+ * caller arrays so that the caller can replay them into its own logger.
+ * --------------------------------------------------------------------------- */
+#define MSN_EV_MINIMUM_SCALE 1   /* a = min_scale */
+#define MSN_EV_MAXIMUM_SCALE 2   /* a = max_scale */
+#define MSN_EV_SCALE_EMPTY 3     /* a = scale_adjust */
+#define MSN_EV_NO_COEFFICIENTS 4 /* no significant wavelet coefficients */
+#define MSN_EV_MINOR_DONE 5      /* a = minor iterations, b = MSN_MINOR_* outcome, v = SNR */
+#define MSN_EV_ALL_SCALES_POOR 6
+#define MSN_EV_REVERTED 7        /* residual worsened: model change undone */
+#define MSN_EV_MAJOR_DONE 8      /* a = major iterations so far */
+#define MSN_EV_NO_WORK 9         /* the run did no work: complete */
+
+typedef struct msn_event {
+    int code, a, b, reserved;
+    double v;
+} msn_event;
+
+typedef struct msn_major_record {
+    int major, max_scale, scale_adjust, minor, outcome, reverted;
+    double snr, std;
+} msn_major_record;
+
+typedef struct msn_moresane_args {
+    int n;                   /* dirty image side */
+    int ns;                  /* subregion side; the subregion starts at off = n/2 - ns/2 */
+    int off;
+    int scale_count;
+    int m_sub, m_data;       /* FFT sides of spec_sub / spec_data */
+    int linear;
+    int major_loop_miter, minor_loop_miter;
+    int enforce_positivity, neg_comp;
+    int noise_rects[8];      /* estimate_threshold pixel set (msn_mad_sigma rects) */
+    int reserved;
+    double sigma_level, tolerance, accuracy, flux_threshold;
+    float loop_gain;
+    float reserved_f;
+    const float *dirty;      /* n x n */
+    const float *mask_sub;   /* ns x ns, or NULL */
+    const int *supp_rects;   /* device [scale_count][4] (msn_apply_threshold), or NULL */
+    const float *energies;   /* HOST [scale_count]: ||w_s|| of the PSF subregion (float32) */
+    const void *spec_sub, *spec_data;
+    float *model, *residual; /* n x n outputs */
+    float *dec, *thr, *emask, *esrc, *planes, *ms; /* scale_count x ns x ns */
+    float *x, *xn, *r, *rn, *p, *ap, *tmp, *rec, *masked, *sub; /* ns x ns */
+    float *conv_full;        /* n x n */
+    double *sigma;           /* scale_count */
+    float *pmax;             /* scale_count */
+    double *scal;            /* 5 */
+    double *snr2;            /* 2 */
+    double *std4;            /* 4 */
+    int *neg;                /* 1 */
+    float *fmax;             /* 1 */
+    void *small;             /* >= 16 and >= 4 * scale_count bytes */
+    size_t small_bytes;
+    void *iuwt_work;         /* msn_iuwt_workspace_bytes(ns, ns) */
+    size_t iuwt_work_bytes;
+    void *fft_work;          /* msn_fft_workspace_bytes(ns, m_sub) */
+    size_t fft_work_bytes;
+    void *fft_work_full;     /* msn_fft_workspace_bytes(n, m_data) */
+    size_t fft_work_full_bytes;
+    void *tool_work;         /* msn_toolbox_workspace_bytes(scale_count, ns, ns) */
+    size_t tool_work_bytes;
+    void *red_work;          /* msn_reduce_workspace_bytes() */
+    size_t red_work_bytes;
+} msn_moresane_args;
+
+typedef struct msn_moresane_result {
+    int major;          /* major iterations performed */
+    int complete;       /* the run did no work (main.py:511-514) */
+    int have_residual;  /* residual was written (at least one model update) */
+    int n_records;      /* entries written to records */
+    int n_events;       /* entries written to events */
+    int events_dropped; /* events that did not fit */
+} msn_moresane_result;
+
+/* Runs one MORESANE deconvolution on stream (waits for it). */
+int msn_moresane_run(void *engine, const msn_moresane_args *args, msn_moresane_result *result,
+                     msn_major_record *records, int records_len, msn_event *events, int events_len, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

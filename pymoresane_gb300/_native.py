@@ -62,6 +62,7 @@ SIGNATURES = {
     "msn_minor_engine_create": (c_int, [ctypes.POINTER(c_void_p)]),
     "msn_minor_engine_destroy": (c_int, [c_void_p]),
     "msn_minor_loop": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_void_p]),
+    "msn_moresane_run": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_void_p, c_int, c_void_p]),
 }
 
 MINOR_RUNNING, MINOR_FALSE_DETECTION, MINOR_CONVERGED, MINOR_STALLED, MINOR_ITERATION_CAP = range(5)
@@ -126,3 +127,40 @@ def call(name, *args):
 
 def query(name, *args):
     return getattr(load(), name)(*args)
+
+
+(EV_MINIMUM_SCALE, EV_MAXIMUM_SCALE, EV_SCALE_EMPTY, EV_NO_COEFFICIENTS, EV_MINOR_DONE, EV_ALL_SCALES_POOR,
+ EV_REVERTED, EV_MAJOR_DONE, EV_NO_WORK) = range(1, 10)
+
+
+class Event(ctypes.Structure):
+    """msn_event of include/msn.h."""
+    _fields_ = [("code", c_int), ("a", c_int), ("b", c_int), ("reserved", c_int), ("v", c_double)]
+
+
+class MajorRecord(ctypes.Structure):
+    """msn_major_record of include/msn.h."""
+    _fields_ = [("major", c_int), ("max_scale", c_int), ("scale_adjust", c_int), ("minor", c_int),
+                ("outcome", c_int), ("reverted", c_int), ("snr", c_double), ("std", c_double)]
+
+
+class MoresaneArgs(ctypes.Structure):
+    """msn_moresane_args of include/msn.h."""
+    _fields_ = ([(k, c_int) for k in ("n", "ns", "off", "scale_count", "m_sub", "m_data", "linear",
+                                      "major_loop_miter", "minor_loop_miter", "enforce_positivity", "neg_comp")]
+                + [("noise_rects", c_int * 8), ("reserved", c_int)]
+                + [(k, c_double) for k in ("sigma_level", "tolerance", "accuracy", "flux_threshold")]
+                + [("loop_gain", c_float), ("reserved_f", c_float)]
+                + [(k, c_void_p) for k in ("dirty", "mask_sub", "supp_rects", "energies", "spec_sub", "spec_data",
+                                           "model", "residual", "dec", "thr", "emask", "esrc", "planes", "ms", "x",
+                                           "xn", "r", "rn", "p", "ap", "tmp", "rec", "masked", "sub", "conv_full",
+                                           "sigma", "pmax", "scal", "snr2", "std4", "neg", "fmax", "small")]
+                + [("small_bytes", c_size_t)]
+                + [f for k in ("iuwt_work", "fft_work", "fft_work_full", "tool_work", "red_work")
+                   for f in ((k, c_void_p), (k + "_bytes", c_size_t))])
+
+
+class MoresaneResult(ctypes.Structure):
+    """msn_moresane_result of include/msn.h."""
+    _fields_ = [(k, c_int) for k in ("major", "complete", "have_residual", "n_records", "n_events",
+                                     "events_dropped")]

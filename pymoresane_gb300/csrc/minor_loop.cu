@@ -127,6 +127,7 @@ int ew_grid4(size_t n4) {
 
 constexpr int kHistory = 4096;   // SNR history entries kept per minor loop
 constexpr size_t kMaxGraphs = 64;  // instantiated graphs cached per engine
+constexpr int kScratch = 512;      // pinned doubles for host reads (plane maxima of up to 30 scales etc.)
 
 struct CacheEntry {
     msn_minor_args key;
@@ -141,6 +142,7 @@ struct Engine {
     MinorState *d_state = nullptr;
     double *d_hist = nullptr;
     MinorState *h_state = nullptr;  // pinned
+    double *h_scratch = nullptr;    // pinned, kScratch doubles: scalars read back by the major loop
     cudaStream_t cs[3] = {nullptr, nullptr, nullptr};  // capture streams: top graph, loop body, branch body
     std::vector<CacheEntry> cache;
     unsigned long long tick = 0;
@@ -331,6 +333,7 @@ extern "C" int msn_minor_engine_create(void **engine) {
     if (rc == MSN_OK) rc = check_cuda(cudaMalloc(&e->d_state, sizeof(MinorState)), "state");
     if (rc == MSN_OK) rc = check_cuda(cudaMalloc(&e->d_hist, kHistory * sizeof(double)), "history");
     if (rc == MSN_OK) rc = check_cuda(cudaMallocHost(&e->h_state, sizeof(MinorState)), "host state");
+    if (rc == MSN_OK) rc = check_cuda(cudaMallocHost(&e->h_scratch, kScratch * sizeof(double)), "host scratch");
     for (int i = 0; i < 3 && rc == MSN_OK; ++i)
         rc = check_cuda(cudaStreamCreateWithFlags(&e->cs[i], cudaStreamNonBlocking), "capture stream");
     if (rc != MSN_OK) {
@@ -351,22 +354,18 @@ extern "C" int msn_minor_engine_destroy(void *engine) {
     if (e->d_state) cudaFree(e->d_state);
     if (e->d_hist) cudaFree(e->d_hist);
     if (e->h_state) cudaFreeHost(e->h_state);
+    if (e->h_scratch) cudaFreeHost(e->h_scratch);
     delete e;
     return MSN_OK;
 }
 
-extern "C" int msn_minor_loop(void *engine, const msn_minor_args *args, msn_minor_result *result,
-                              double *snr_history, int history_len, void *stream) {
-    clear_error();
-    Engine *e = static_cast<Engine *>(engine);
-    if (!e || !args || !result) return set_error(MSN_ERR_INVALID, "msn_minor_loop: null engine, arguments or result");
+namespace msn {
+namespace {
+
+// One minor loop on stream st; the caller holds e->mu.
+int run_minor(Engine *e, const msn_minor_args *args, msn_minor_result *result, double *snr_history,
+              int history_len, cudaStream_t st) {
     MSN_TRY(validate_args(args));
-    int device = -1;
-    MSN_TRY(check_cuda(cudaGetDevice(&device), "cudaGetDevice"));
-    if (device != e->device)
-        return set_error(MSN_ERR_INVALID, "msn_minor_loop: engine belongs to device %d, current device is %d",
-                         e->device, device);
-    std::lock_guard<std::mutex> lock(e->mu);
     const msn_minor_args key = make_key(args);
     CacheEntry *ce = nullptr;
     for (auto &c : e->cache)
@@ -390,7 +389,6 @@ extern "C" int msn_minor_loop(void *engine, const msn_minor_args *args, msn_mino
         }
     }
     ce->last_use = ++e->tick;
-    cudaStream_t st = as_stream(stream);
     MSN_TRY(check_cuda(cudaGraphLaunch(ce->exec, st), "graph launch"));
     MSN_TRY(check_cuda(cudaMemcpyAsync(e->h_state, e->d_state, sizeof(MinorState), cudaMemcpyDeviceToHost, st),
                        "read state"));
@@ -401,6 +399,7 @@ extern "C" int msn_minor_loop(void *engine, const msn_minor_args *args, msn_mino
     result->minor = s.minor;
     result->outcome = s.outcome;
     result->positivity_runs = s.positivity_runs;
+    result->reserved = 0;
     result->snr_current = s.snr_current;
     result->snr_last = s.snr_last;
     if (snr_history && history_len > 0) {
@@ -411,4 +410,279 @@ extern "C" int msn_minor_loop(void *engine, const msn_minor_args *args, msn_mino
                                "read SNR history"));
     }
     return MSN_OK;
+}
+
+int check_engine_device(Engine *e) {
+    int device = -1;
+    MSN_TRY(check_cuda(cudaGetDevice(&device), "cudaGetDevice"));
+    if (device != e->device)
+        return set_error(MSN_ERR_INVALID, "engine belongs to device %d, current device is %d", e->device, device);
+    return MSN_OK;
+}
+
+}  // namespace
+}  // namespace msn
+
+extern "C" int msn_minor_loop(void *engine, const msn_minor_args *args, msn_minor_result *result,
+                              double *snr_history, int history_len, void *stream) {
+    clear_error();
+    Engine *e = static_cast<Engine *>(engine);
+    if (!e || !args || !result) return set_error(MSN_ERR_INVALID, "msn_minor_loop: null engine, arguments or result");
+    MSN_TRY(check_engine_device(e));
+    std::lock_guard<std::mutex> lock(e->mu);
+    return run_minor(e, args, result, snr_history, history_len, as_stream(stream));
+}
+
+// ---------------------------------------------------------------------------
+// Major loop (pymoresane/main.py:266-514)
+// ---------------------------------------------------------------------------
+namespace msn {
+namespace {
+
+struct EventLog {
+    msn_event *ev;
+    int cap, n = 0, dropped = 0;
+    void add(int code, int a = 0, int b = 0, double v = 0.0) {
+        if (ev && n < cap) {
+            ev[n].code = code;
+            ev[n].a = a;
+            ev[n].b = b;
+            ev[n].reserved = 0;
+            ev[n].v = v;
+            ++n;
+        } else {
+            ++dropped;
+        }
+    }
+};
+
+// numpy.argmax of x[from:]: the first maximum, a NaN counting as the maximum.
+int first_argmax(const std::vector<float> &x, int from) {
+    int best = from;
+    for (int i = from; i < (int)x.size(); ++i) {
+        if (std::isnan(x[i])) return i;
+        if (x[i] > x[best]) best = i;
+    }
+    return best;
+}
+
+int validate_run(const msn_moresane_args *a) {
+    static const char *fn = "msn_moresane_run";
+    if (a->n <= 0 || a->n % 4 || a->ns <= 0 || a->ns % 4 || a->ns > a->n || a->off < 0 || a->off + a->ns > a->n)
+        return set_error(MSN_ERR_INVALID, "%s: bad sides n=%d ns=%d off=%d", fn, a->n, a->ns, a->off);
+    if (a->scale_count < 1 || a->scale_count > 30 || (1LL << a->scale_count) > a->ns)
+        return set_error(MSN_ERR_INVALID, "%s: bad scale_count %d for side %d", fn, a->scale_count, a->ns);
+    if (a->scale_count > kScratch / 2) return set_error(MSN_ERR_INVALID, "%s: too many scales", fn);
+    const void *ptrs[] = {a->dirty, a->energies, a->spec_sub, a->spec_data, a->model, a->residual, a->dec, a->thr,
+                          a->emask, a->esrc, a->planes, a->ms, a->x, a->xn, a->r, a->rn, a->p, a->ap, a->tmp,
+                          a->rec, a->masked, a->sub, a->conv_full, a->sigma, a->pmax, a->scal, a->snr2, a->std4,
+                          a->neg, a->fmax, a->small, a->iuwt_work, a->fft_work, a->fft_work_full, a->tool_work,
+                          a->red_work};
+    for (const void *p : ptrs)
+        if (!p) return set_error(MSN_ERR_INVALID, "%s: null buffer in the argument block", fn);
+    return MSN_OK;
+}
+
+int read_back(Engine *e, const void *d_src, size_t bytes, cudaStream_t st) {
+    MSN_TRY(check_cuda(cudaMemcpyAsync(e->h_scratch, d_src, bytes, cudaMemcpyDeviceToHost, st), "read back"));
+    return check_cuda(cudaStreamSynchronize(st), "major loop");
+}
+
+int run_moresane(Engine *e, const msn_moresane_args *a, msn_moresane_result *res, msn_major_record *records,
+                 int records_len, EventLog &ev, cudaStream_t st) {
+    const int n = a->n, ns = a->ns, o = a->off, S = a->scale_count;
+    const size_t nvec = (size_t)ns * ns, nfull = (size_t)n * n;
+    const float *dirty_sub = a->sub;
+    // dirty_sub = dirty[o:o+ns, o:o+ns] (main.py:249-253); the whole image when ns == n
+    auto sub_view = [&](const float *img) -> int {
+        if (ns == n) {
+            dirty_sub = img;
+            return MSN_OK;
+        }
+        dirty_sub = a->sub;
+        return check_cuda(cudaMemcpy2DAsync(a->sub, ns * sizeof(float), img + (size_t)o * n + o, n * sizeof(float),
+                                            ns * sizeof(float), ns, cudaMemcpyDeviceToDevice, st),
+                          "subregion copy");
+    };
+    // residual = dirty - H * model over the whole image with the data PSF (main.py:483-486)
+    auto residual_of = [&]() -> int {
+        MSN_TRY(msn_fft_convolve(a->model, n, a->m_data, a->spec_data, a->conv_full, a->linear, a->fft_work_full,
+                                 a->fft_work_full_bytes, st));
+        return msn_sub(a->dirty, a->conv_full, a->residual, nfull, st);
+    };
+    auto dirty_peak = [&](float *out) -> int {
+        MSN_TRY(msn_plane_max(dirty_sub, 1, nvec, 0, a->fmax, a->small, a->small_bytes, st));
+        MSN_TRY(read_back(e, a->fmax, sizeof(float), st));
+        *out = *reinterpret_cast<const float *>(e->h_scratch);
+        return MSN_OK;
+    };
+
+    MSN_TRY(check_cuda(cudaMemsetAsync(a->model, 0, nfull * sizeof(float), st), "zero model"));
+    MSN_TRY(sub_view(a->dirty));
+    int major = 0, min_scale = 0, n_rec = 0;
+    float max_coeff = 1.0f;
+    double std_current = 1000.0, std_ratio = 1.0;
+    bool have_x = false, have_residual = false;
+    std::vector<float> normalised(S, 0.0f);
+    res->complete = 0;
+
+    msn_minor_args m;
+    std::memset(&m, 0, sizeof(m));
+    m.n = ns;
+    m.m = a->m_sub;
+    m.linear = a->linear;
+    m.minor_loop_miter = a->minor_loop_miter;
+    m.enforce_positivity = a->enforce_positivity;
+    m.spec = a->spec_sub;
+    m.rec = a->rec;
+    m.x = a->x;
+    m.xn = a->xn;
+    m.r = a->r;
+    m.rn = a->rn;
+    m.p = a->p;
+    m.ap = a->ap;
+    m.tmp = a->tmp;
+    m.planes = a->planes;
+    m.emask = a->emask;
+    m.esrc = a->esrc;
+    m.ms = a->ms;
+    m.scal = a->scal;
+    m.snr2 = a->snr2;
+    m.neg = a->neg;
+    m.fft_work = a->fft_work;
+    m.fft_work_bytes = a->fft_work_bytes;
+    m.iuwt_work = a->iuwt_work;
+    m.iuwt_work_bytes = a->iuwt_work_bytes;
+    m.red_work = a->red_work;
+    m.red_work_bytes = a->red_work_bytes;
+
+    while (true) {
+        if (!(major < a->major_loop_miter && max_coeff > 0 && std_ratio > a->accuracy)) break;
+        float peak = 0.0f;
+        MSN_TRY(dirty_peak(&peak));
+        if (!(peak > a->flux_threshold)) break;
+        msn_major_record rec;
+        std::memset(&rec, 0, sizeof(rec));
+        rec.major = major;
+        while (min_scale < S) {
+            if (min_scale == 0) {
+                // threshold at sigma_level MAD sigmas of the (unmasked) decomposition (main.py:279-296)
+                MSN_TRY(msn_iuwt_decompose(dirty_sub, a->dec, nullptr, ns, ns, S, 0, a->iuwt_work, a->iuwt_work_bytes,
+                                           st));
+                MSN_TRY(msn_mad_sigma(a->dec, S, ns, ns, a->noise_rects, a->sigma, a->tool_work, a->tool_work_bytes,
+                                      st));
+                if (a->mask_sub) {
+                    MSN_TRY(msn_mul(dirty_sub, a->mask_sub, a->masked, nvec, st));
+                    MSN_TRY(msn_iuwt_decompose(a->masked, a->dec, nullptr, ns, ns, S, 0, a->iuwt_work,
+                                               a->iuwt_work_bytes, st));
+                }
+                MSN_TRY(msn_apply_threshold(a->dec, S, ns, ns, a->sigma, a->sigma_level, a->supp_rects, a->thr,
+                                            a->pmax, a->small, a->small_bytes, st));
+                MSN_TRY(read_back(e, a->pmax, S * sizeof(float), st));
+                const float *pm = reinterpret_cast<const float *>(e->h_scratch);
+                for (int i = 0; i < S; ++i) normalised[i] = pm[i] / a->energies[i];
+            }
+            const int max_index = first_argmax(normalised, min_scale);
+            const int max_scale = max_index + 1;
+            max_coeff = normalised[max_index];
+            if (max_coeff == 0.0f) {
+                ev.add(MSN_EV_NO_COEFFICIENTS);
+                break;
+            }
+            ev.add(MSN_EV_MINIMUM_SCALE, min_scale);
+            ev.add(MSN_EV_MAXIMUM_SCALE, max_scale);
+            int scale_adjust = 0;
+            for (int i = max_index - 1; i >= 0; --i) {
+                if (normalised[i] == 0.0f) {
+                    scale_adjust = i + 1;
+                    ev.add(MSN_EV_SCALE_EMPTY, scale_adjust);
+                    break;
+                }
+            }
+            const int planes = max_scale - scale_adjust;
+            MSN_TRY(msn_source_extraction(a->thr + (size_t)scale_adjust * nvec, planes, ns, ns, (float)a->tolerance,
+                                          a->neg_comp, a->emask, a->esrc, a->tool_work, a->tool_work_bytes, st));
+            MSN_TRY(msn_iuwt_recompose(a->esrc, planes, nullptr, a->rec, ns, ns, scale_adjust, a->iuwt_work,
+                                       a->iuwt_work_bytes, st));
+            m.max_scale = max_scale;
+            m.scale_adjust = scale_adjust;
+            msn_minor_result mr;
+            MSN_TRY(run_minor(e, &m, &mr, nullptr, 0, st));
+            if (mr.outcome == MSN_MINOR_FALSE_DETECTION) {
+                min_scale += 1;
+            } else if (mr.outcome == MSN_MINOR_CONVERGED) {
+                min_scale = 0;
+            } else if (mr.outcome == MSN_MINOR_STALLED) {
+                min_scale = mr.snr_current > 10.5 ? 0 : min_scale + 1;
+            }
+            ev.add(MSN_EV_MINOR_DONE, mr.minor, mr.outcome, mr.snr_current);
+            have_x = true;
+            rec.max_scale = max_scale;
+            rec.scale_adjust = scale_adjust;
+            rec.minor = mr.minor;
+            rec.outcome = mr.outcome;
+            rec.snr = mr.snr_current;
+            if (mr.minor == a->minor_loop_miter && mr.snr_current > 10.5) {
+                min_scale = 0;
+                break;
+            }
+            if (min_scale == 0) break;
+        }
+        if (min_scale == S) {
+            ev.add(MSN_EV_ALL_SCALES_POOR);
+            break;
+        }
+        if (max_coeff > 0 && have_x) {
+            // model += gain x; residual; revert when the residual's deviation grew (main.py:466-503)
+            MSN_TRY(msn_model_update(a->model, n, a->x, ns, o, o, a->loop_gain, 1, st));
+            MSN_TRY(residual_of());
+            have_residual = true;
+            const double std_last = std_current;
+            MSN_TRY(msn_region_std(a->residual, n, ns, ns, o, o, a->std4, a->red_work, a->red_work_bytes, st));
+            MSN_TRY(read_back(e, a->std4 + 3, sizeof(double), st));
+            std_current = e->h_scratch[0];
+            std_ratio = (std_last - std_current) / std_last;
+            rec.std = std_current;
+            rec.reverted = std_ratio < 0;
+            if (std_ratio < 0) {
+                ev.add(MSN_EV_REVERTED);
+                MSN_TRY(msn_model_update(a->model, n, a->x, ns, o, o, a->loop_gain, -1, st));
+                MSN_TRY(residual_of());
+            }
+            MSN_TRY(sub_view(a->residual));
+            major += 1;
+            if (records && n_rec < records_len) records[n_rec++] = rec;
+            ev.add(MSN_EV_MAJOR_DONE, major);
+        }
+        if (major == 0) {
+            ev.add(MSN_EV_NO_WORK);
+            res->complete = 1;
+            break;
+        }
+    }
+    MSN_TRY(check_cuda(cudaStreamSynchronize(st), "major loop"));
+    res->major = major;
+    res->have_residual = have_residual;
+    res->n_records = n_rec;
+    return MSN_OK;
+}
+
+}  // namespace
+}  // namespace msn
+
+extern "C" int msn_moresane_run(void *engine, const msn_moresane_args *args, msn_moresane_result *result,
+                                msn_major_record *records, int records_len, msn_event *events, int events_len,
+                                void *stream) {
+    clear_error();
+    Engine *e = static_cast<Engine *>(engine);
+    if (!e || !args || !result) return set_error(MSN_ERR_INVALID, "msn_moresane_run: null engine, arguments or result");
+    std::memset(result, 0, sizeof(*result));
+    MSN_TRY(validate_run(args));
+    MSN_TRY(check_engine_device(e));
+    std::lock_guard<std::mutex> lock(e->mu);
+    EventLog ev{events, events ? events_len : 0};
+    const int rc = run_moresane(e, args, result, records, records ? records_len : 0, ev, as_stream(stream));
+    result->n_events = ev.n;
+    result->events_dropped = ev.dropped;
+    return rc;
 }

@@ -16,6 +16,7 @@ has no CPU implementation). See INTEGRATION.md for every difference.
 import ctypes
 import logging
 import math
+import threading
 
 import numpy as np
 import torch
@@ -65,7 +66,8 @@ class _Buffers:
         self.esrc = torch.empty((s, ns, ns), **f32)
         self.planes = torch.empty((s, ns, ns), **f32)
         self.ms = torch.empty((s, ns, ns), **f32)   # running model sources mask * W(H x)
-        self.vec = {k: torch.empty((ns, ns), **f32) for k in ("x", "xn", "r", "rn", "p", "ap", "tmp", "rec")}
+        self.vec = {k: torch.empty((ns, ns), **f32)
+                    for k in ("x", "xn", "r", "rn", "p", "ap", "tmp", "rec", "masked", "sub")}
         self.conv_full = torch.empty((n_full, n_full), **f32)
         self.iuwt_work = dev.iuwt_workspace(ns, ns, device)
         self.fft_work = dev.fft_workspace(ns, m_sub, device)
@@ -78,6 +80,56 @@ class _Buffers:
         self.neg = torch.zeros(1, dtype=torch.int32, device=device)
         self.small = torch.empty(256, dtype=torch.uint8, device=device)
         self.fmax = torch.empty(1, dtype=torch.float32, device=device)
+        self.sigma = torch.empty(s, dtype=torch.float64, device=device)
+        self.pmax = torch.empty(s, dtype=torch.float32, device=device)
+
+
+_ENGINES = threading.local()
+
+
+def _thread_engine(device):
+    """The calling thread's minor-loop engine for ``device``, created on first use and kept.
+
+    Its graph cache is keyed by every buffer address, so a later Deconvolver
+    whose buffers land at the same addresses re-uses the captured graphs.
+    """
+    engines = getattr(_ENGINES, "by_device", None)
+    if engines is None:
+        engines = _ENGINES.by_device = {}
+    key = device.index
+    if key not in engines:
+        h = ctypes.c_void_p()
+        _native.call("msn_minor_engine_create", ctypes.byref(h))
+        engines[key] = h
+    return engines[key]
+
+
+def _replay(events):
+    """Emit the log messages of a native run, in order (texts of pymoresane/main.py)."""
+    for e in events:
+        c = e.code
+        if c == _native.EV_MINIMUM_SCALE:
+            logger.info("Minimum scale = %d", e.a)
+        elif c == _native.EV_MAXIMUM_SCALE:
+            logger.info("Maximum scale = %d", e.a)
+        elif c == _native.EV_SCALE_EMPTY:
+            logger.info("Scale %d is empty. Ignoring scales <= %d", e.a, e.a)
+        elif c == _native.EV_NO_COEFFICIENTS:
+            logger.info("No significant wavelet coefficients detected.")
+        elif c == _native.EV_MINOR_DONE:
+            if e.b == _native.MINOR_FALSE_DETECTION:
+                logger.info("SNR too large on first iteration - false detection. Incrementing the minimum scale.")
+            elif e.b == _native.MINOR_CONVERGED:
+                logger.info("Model has reached <1% error - exiting minor loop.")
+            logger.info("%d minor loop iterations performed.", e.a)
+        elif c == _native.EV_ALL_SCALES_POOR:
+            logger.info("All scales are performing poorly - stopping.")
+        elif c == _native.EV_REVERTED:
+            logger.info("Residual has worsened - reverting changes.")
+        elif c == _native.EV_MAJOR_DONE:
+            logger.info("%d major loop iterations performed.", e.a)
+        elif c == _native.EV_NO_WORK:
+            logger.info("Current MORESANE iteration did no work - finished.")
 
 
 class Deconvolver:
@@ -108,7 +160,9 @@ class Deconvolver:
         # device (msn_minor_loop); False: the host drives every iteration, as the
         # reference does (pymoresane/main.py:365-457).
         self.native_minor_loop = True
-        self._engine = None
+        # True: the whole major loop runs inside libmsn (msn_moresane_run), one call
+        # per deconvolution; needs native_minor_loop. False: this module drives it.
+        self.native_major_loop = True
         self._psf_cache = _PsfCache()
         self._bufs = {}
         # A Workspace (pymoresane_gb300.batch) shared by the deconvolutions that one
@@ -183,11 +237,7 @@ class Deconvolver:
     def _engine_handle(self):
         if self.workspace is not None:
             return self.workspace.engine()
-        if self._engine is None:
-            h = ctypes.c_void_p()
-            _native.call("msn_minor_engine_create", ctypes.byref(h))
-            self._engine = h
-        return self._engine
+        return _thread_engine(self.device)
 
     def _native_minor(self, B, V, spec_sub, linear, max_scale, scale_adjust, planes, ns, miter, positivity, st):
         """One minor loop through msn_minor_loop; returns (MinorResult, per-iteration SNRs)."""
@@ -211,13 +261,52 @@ class Deconvolver:
         _native.call("msn_minor_loop", engine, ctypes.byref(a), ctypes.byref(res), hist, len(hist), st)
         return res, list(hist[:min(res.minor, len(hist))])
 
-    def __del__(self):
-        eng, self._engine = getattr(self, "_engine", None), None
-        if eng is not None:
-            try:
-                _native.query("msn_minor_engine_destroy", eng)
-            except Exception:
-                pass
+    def _native_run(self, dirty, B, spec_sub, spec_data, energies, mask_sub, supp, n, ns, o, scale_count, linear,
+                    sigma_level, loop_gain, tolerance, accuracy, major_loop_miter, minor_loop_miter,
+                    enforce_positivity, flux_threshold, neg_comp, edge_excl, int_excl, st):
+        """The major loop through msn_moresane_run; log events are replayed into this module's logger."""
+        engine = self._engine_handle()
+        model = torch.empty((n, n), dtype=torch.float32, device=dirty.device)
+        residual = torch.empty((n, n), dtype=torch.float32, device=dirty.device)
+        energies_h = np.ascontiguousarray(energies, dtype=np.float32)
+        V = B.vec
+        a = _native.MoresaneArgs()
+        a.n, a.ns, a.off, a.scale_count = n, ns, o, scale_count
+        a.m_sub, a.m_data, a.linear = spec_sub.m, spec_data.m, 1 if linear else 0
+        a.major_loop_miter, a.minor_loop_miter = int(major_loop_miter), int(minor_loop_miter)
+        a.enforce_positivity, a.neg_comp = 1 if enforce_positivity else 0, 1 if neg_comp else 0
+        a.noise_rects[:] = dev.noise_rects(ns, ns, edge_excl, int_excl)
+        a.sigma_level, a.tolerance, a.accuracy = float(sigma_level), float(tolerance), float(accuracy)
+        a.flux_threshold, a.loop_gain = float(flux_threshold), float(loop_gain)
+        a.dirty = dirty.data_ptr()
+        a.mask_sub = None if mask_sub is None else mask_sub.data_ptr()
+        a.supp_rects = None if supp is None else supp.data_ptr()
+        a.energies = energies_h.ctypes.data
+        a.spec_sub = (B.spec_slot if self.workspace is not None else spec_sub.packed).data_ptr()
+        a.spec_data = spec_data.packed.data_ptr()
+        a.model, a.residual = model.data_ptr(), residual.data_ptr()
+        for k in ("dec", "thr", "emask", "esrc", "planes", "ms", "conv_full", "sigma", "pmax", "scal", "snr2",
+                  "std4", "neg", "fmax", "small"):
+            setattr(a, k, getattr(B, k).data_ptr())
+        for k in ("x", "xn", "r", "rn", "p", "ap", "tmp", "rec", "masked", "sub"):
+            setattr(a, k, V[k].data_ptr())
+        a.small_bytes = B.small.numel()
+        for k in ("iuwt_work", "fft_work", "fft_work_full", "tool_work", "red_work"):
+            w = getattr(B, k)
+            setattr(a, k, w.data_ptr())
+            setattr(a, k + "_bytes", w.numel())
+        res = _native.MoresaneResult()
+        cap = max(1, int(major_loop_miter))
+        records = (_native.MajorRecord * cap)()
+        events = (_native.Event * (cap * (4 * scale_count + 8) + 8))()
+        _native.call("msn_moresane_run", engine, ctypes.byref(a), ctypes.byref(res), records, cap, events,
+                     len(events), st)
+        _replay(events[:res.n_events])
+        for r in records[:res.n_records]:
+            self.log.append({"major": r.major, "max_scale": r.max_scale, "scale_adjust": r.scale_adjust,
+                             "minor": r.minor, "snr": r.snr, "std": r.std, "reverted": bool(r.reverted)})
+        self.complete = bool(res.complete)
+        return model, (residual if res.have_residual else None), res.major
 
     def moresane(self, dirty, subregion=None, scale_count=None, sigma_level=4, loop_gain=0.1, tolerance=0.75,
                  accuracy=1e-6, major_loop_miter=100, minor_loop_miter=30, conv_mode='linear',
@@ -272,6 +361,12 @@ class Deconvolver:
                 y0, y1 = _rects_for(slice(e, -e), ns)
                 rects.append([y0, y1, y0, y1])
             supp = torch.tensor(rects, dtype=torch.int32, device=dirty.device)
+
+        if self.native_major_loop and self.native_minor_loop:
+            return self._native_run(dirty, B, spec_sub, spec_data, energies, mask_sub, supp, n, ns, o, scale_count,
+                                    linear, sigma_level, loop_gain, tolerance, accuracy, major_loop_miter,
+                                    minor_loop_miter, enforce_positivity, flux_threshold, neg_comp, edge_excl,
+                                    int_excl, st)
 
         def sub_view(img):
             return img if ns == n else img[o:o + ns, o:o + ns].contiguous()

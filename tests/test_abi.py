@@ -52,12 +52,14 @@ def test_host_queries(lib):
 
 
 def test_minor_structs_match_header(tmp_path):
-    """The ctypes mirrors of msn_minor_args / msn_minor_result have the C layout (gcc on the header)."""
+    """The ctypes mirrors of the engine structs have the C layout (gcc on the header)."""
     import shutil
     import subprocess
     if shutil.which("gcc") is None:
         pytest.skip("gcc not available")
-    structs = {"msn_minor_args": _native.MinorArgs, "msn_minor_result": _native.MinorResult}
+    structs = {"msn_minor_args": _native.MinorArgs, "msn_minor_result": _native.MinorResult,
+               "msn_moresane_args": _native.MoresaneArgs, "msn_moresane_result": _native.MoresaneResult,
+               "msn_major_record": _native.MajorRecord, "msn_event": _native.Event}
     lines = ["#include <stdio.h>", "#include <stddef.h>", '#include "msn.h"', "int main(void) {"]
     for cname, cls in structs.items():
         lines.append(f'printf("{cname} size %zu\\n", sizeof({cname}));')

@@ -141,3 +141,35 @@ def test_native_minor_loop_matches_host_loop(cuda, name):
     assert [(r["max_scale"], r["scale_adjust"], r["minor"]) for r in la] == \
            [(r["max_scale"], r["scale_adjust"], r["minor"]) for r in lb]
     assert np.max(np.abs(ma - mb)) <= MODEL_TOL * np.max(np.abs(mb))
+
+
+@pytest.mark.parametrize("name", ["lin_double", "circ_pos", "neg_excl"])
+def test_native_major_loop_matches_host_major_loop(cuda, name, caplog):
+    # The whole major loop inside libmsn (msn_moresane_run) against this package's
+    # host-driven major loop over the same calls: identical model, residual, records
+    # and log messages.
+    import logging
+
+    from pymoresane_gb300.main import Deconvolver
+    import torch
+    g = np.load(os.path.join(GOLDEN, "moresane.npz"))
+    pk, rk = mg.MORESANE_CASES[name]
+    kw = dict(mg.RUN_DEFAULTS, **rk)
+    dirty = torch.from_numpy(g[f"{name}_dirty"]).cuda()
+    runs = []
+    for native in (True, False):
+        caplog.clear()
+        with caplog.at_level(logging.INFO, logger="pymoresane_gb300.main"):
+            eng = Deconvolver(g[f"{name}_psf"])
+            eng.native_major_loop = native
+            model, residual, major = eng.moresane(dirty, **kw)
+        msgs = [r.getMessage() for r in caplog.records if r.levelno >= logging.INFO]
+        runs.append((model.cpu().numpy(), None if residual is None else residual.cpu().numpy(), major, eng.log,
+                     msgs, eng.complete))
+    (ma, ra, ka, la, ga, ca), (mb, rb, kb, lb, gb, cb) = runs
+    assert ka == kb and ca == cb
+    assert np.array_equal(ma, mb)
+    assert (ra is None) == (rb is None) and (ra is None or np.array_equal(ra, rb))
+    keys = ("major", "max_scale", "scale_adjust", "minor", "reverted")
+    assert [[r[k] for k in keys] for r in la] == [[r[k] for k in keys] for r in lb]
+    assert ga == gb
