@@ -179,6 +179,69 @@ __device__ __forceinline__ void fused_product(float2 *__restrict__ buf, const fl
     __syncthreads();
 }
 
+// First pass (Ns = 1, no twiddles) fed from registers: load(n) returns
+// sequence element n (global loads, zero padding, Hermitian extension ...).
+// Writes the pass output to the team's shared-memory sequence.
+template <bool INV, int M, class Load>
+__device__ __forceinline__ void first_pass_load(float2 *__restrict__ buf, Load load, int t) {
+    constexpr int E = P<M>::E, R = P<M>::plan.radix[0];
+    constexpr int NB = E / R, TEAM = P<M>::TEAM, STRIDE = M / R;
+    static_assert(P<M>::plan.ns[0] == 1 && 16 % R == 0, "first pass must be Ns = 1 with R dividing 16");
+    float2 v[E];
+#pragma unroll
+    for (int b = 0; b < NB; ++b) {
+        const int j = t + b * TEAM;
+#pragma unroll
+        for (int r = 0; r < R; ++r) v[b * R + r] = load(j + r * STRIDE);
+    }
+#pragma unroll
+    for (int b = 0; b < NB; ++b) {
+        const int j = t + b * TEAM;
+        dft<INV, R>(v + b * R);
+        float2 *s = buf + sidx(j * R);
+#pragma unroll
+        for (int r = 0; r < R; ++r) s[r] = v[b * R + out_slot<R>(r)];
+    }
+    __syncthreads();
+}
+
+// Last pass (Ns = M / R) from the team's shared-memory sequence to
+// store(n, X[n]) for every output element n (no shared-memory write back).
+template <bool INV, int M, class Store>
+__device__ __forceinline__ void last_pass_store(const float2 *__restrict__ buf, const float2 *__restrict__ tw,
+                                                Store store, int t) {
+    constexpr int Q = P<M>::NP - 1;
+    constexpr int E = P<M>::E, R = P<M>::plan.radix[Q], NS = P<M>::plan.ns[Q];
+    constexpr int NB = E / R, TEAM = P<M>::TEAM, STRIDE = M / R;
+    static_assert(NS == STRIDE && STRIDE % 16 == 0, "last pass must have Ns = M / R");
+    float2 v[E];
+#pragma unroll
+    for (int b = 0; b < NB; ++b) {
+        const int j = t + b * TEAM;
+        const float2 *s = buf + sidx(j);
+#pragma unroll
+        for (int r = 0; r < R; ++r) v[b * R + r] = s[pad_off(r * STRIDE)];
+    }
+#pragma unroll
+    for (int b = 0; b < NB; ++b) {
+        const int j = t + b * TEAM;  // k = j mod Ns = j
+        const float2 *w = tw + P<M>::plan.twbase[Q] + j * (R - 1) - 1;
+#pragma unroll
+        for (int r = 1; r < R; ++r) v[b * R + r] = cmul(v[b * R + r], INV ? cconj(w[r]) : w[r]);
+        dft<INV, R>(v + b * R);
+#pragma unroll
+        for (int r = 0; r < R; ++r) store(j + r * NS, v[b * R + out_slot<R>(r)]);
+    }
+}
+
+// Plans whose first pass has Ns = 1 with a radix dividing 16 and whose last pass
+// has Ns = M / R on 16-element blocks (every plan with at least two passes).
+template <int M>
+constexpr bool direct_ok() {
+    return P<M>::NP >= 2 && P<M>::plan.ns[0] == 1 && 16 % P<M>::plan.radix[0] == 0 &&
+           (M / P<M>::plan.radix[P<M>::NP - 1]) % 16 == 0;
+}
+
 // --------------------------------------------------------------------------
 // 1. Row R2C: rows [2q, 2q+1] of a real nrows x ncols image placed at column
 //    offset col_off of the M-point row; writes W = M/2 + 1 bins per row.
@@ -321,6 +384,125 @@ conv_cols(const float2 *__restrict__ in, InL in_lay, int in_rows, int in_off, co
     }
 }
 
+// Column convolution with global-fed first pass and global-written last pass:
+// one shared-memory sequence per column (no staging copies, no double buffer),
+// so two or more CTAs fit on an SM. Requires a fusable plan.
+template <int M, class InL, class OutL>
+__global__ void __launch_bounds__(P<M>::C * P<M>::TEAM)
+conv_cols_direct(const float2 *__restrict__ in, InL in_lay, int in_rows, int in_off, const float2 *__restrict__ h,
+                 float2 *__restrict__ out, OutL out_lay, int out_rows, int shift) {
+    extern __shared__ float2 smem[];
+    constexpr int TEAM = P<M>::TEAM, PLEN = P<M>::PLEN, C = P<M>::C, W = M / 2 + 1, GROUPS = P<M>::plan.groups;
+    constexpr int NP = P<M>::NP;
+    static_assert(P<M>::plan.fusable && NP >= 2, "conv_cols_direct needs a fusable plan");
+    const int cc = threadIdx.x / TEAM, t = threadIdx.x - cc * TEAM;
+    float2 *tw = smem;
+    build_twiddles<M>(tw);
+    float2 *buf = smem + P<M>::TW_WORDS + cc * PLEN;
+    __syncthreads();
+    for (int g = blockIdx.x; g < GROUPS; g += gridDim.x) {
+        const int col = g * C + cc;
+        const bool in_valid = in_lay.valid(col, W), out_valid = out_lay.valid(col, W);
+        // sequence position n is input row n - in_off when that row exists, zero otherwise
+        first_pass_load<false, M>(buf, [&](int n) {
+            const int row = n - in_off;
+            return (in_valid && row >= 0 && row < in_rows) ? __ldg(in + in_lay.at(row, col)) : make_float2(0.f, 0.f);
+        }, t);
+        passes<false, M, 1, NP - 1>(buf, tw, t);
+        fused_product<M>(buf, tw, h + (size_t)g * M * C, cc, t);
+        passes<true, M, 1, NP - 1>(buf, tw, t);
+        // output row i takes sequence position (i + shift) mod M
+        last_pass_store<true, M>(buf, tw, [&](int n, float2 v) {
+            int i = n - shift;
+            if (i < 0) i += M;
+            if (out_valid && i < out_rows) out[out_lay.at(i, col)] = v;
+        }, t);
+        __syncthreads();
+    }
+}
+
+// Row R2C with the first pass fed from the image rows (two real rows packed as
+// one complex sequence, zero outside [col_off, col_off + ncols)); one
+// shared-memory sequence per team. The loop over row pairs is uniform across
+// the CTA (teams past the last pair compute zeros and store nothing).
+template <int M, class OutL>
+__global__ void __launch_bounds__(512)
+rfft_rows_direct(const float *__restrict__ x, int nrows, int ncols, int col_off, float2 *__restrict__ out, OutL lay) {
+    extern __shared__ float2 smem[];
+    constexpr int TEAM = P<M>::TEAM, PLEN = P<M>::PLEN, W = M / 2 + 1, NP = P<M>::NP;
+    const int p = threadIdx.x / TEAM, t = threadIdx.x - p * TEAM, teams = blockDim.x / TEAM;
+    float2 *tw = smem;
+    build_twiddles<M>(tw);
+    float2 *buf = smem + P<M>::TW_WORDS + p * PLEN;
+    __syncthreads();
+    const int npairs = (nrows + 1) / 2;
+    for (int pair0 = blockIdx.x * teams; pair0 < npairs; pair0 += gridDim.x * teams) {
+        const int ra = 2 * (pair0 + p), rb = ra + 1;
+        const bool ha = ra < nrows, hb = rb < nrows;
+        first_pass_load<false, M>(buf, [&](int n) {
+            const int c = n - col_off;
+            const bool in_row = c >= 0 && c < ncols;
+            return make_float2(ha && in_row ? __ldg(x + (size_t)ra * ncols + c) : 0.f,
+                               hb && in_row ? __ldg(x + (size_t)rb * ncols + c) : 0.f);
+        }, t);
+        passes<false, M, 1, NP>(buf, tw, t);
+        for (int k = t; k < W; k += TEAM) {
+            const float2 zk = buf[sidx(k)];
+            const float2 zm = buf[sidx(k == 0 ? 0 : M - k)];
+            // Xa = (Z[k] + conj Z[M-k]) / 2, Xb = (Z[k] - conj Z[M-k]) / (2i)
+            if (ha) out[lay.at(ra, k)] = make_float2(0.5f * (zk.x + zm.x), 0.5f * (zk.y - zm.y));
+            if (hb) out[lay.at(rb, k)] = make_float2(0.5f * (zk.y + zm.y), -0.5f * (zk.x - zm.x));
+        }
+        __syncthreads();
+    }
+}
+
+// Row C2R of Hermitian half-rows [2q, 2q+1] with the first inverse pass fed from
+// the half spectra (Z = Xa + i Xb extended by Hermitian symmetry) and the last
+// pass writing the shifted, cropped, scaled real rows; one shared-memory
+// sequence per team.
+// Measured on GB300 at M = 4096: left free to use 128 registers (one 512-thread
+// CTA per SM, all 32 first-pass loads in flight) it beats both a 64-register
+// bound (two CTAs per SM, loads serialised) and the staged cp.async version.
+template <int M, class InL>
+__global__ void __launch_bounds__(512)
+irfft_rows_direct(const float2 *__restrict__ in, InL lay, int nrows, float *__restrict__ out, int out_cols,
+                  int shift, float div) {
+    extern __shared__ float2 smem[];
+    constexpr int TEAM = P<M>::TEAM, PLEN = P<M>::PLEN, HALF = M / 2, NP = P<M>::NP;
+    const int p = threadIdx.x / TEAM, t = threadIdx.x - p * TEAM, teams = blockDim.x / TEAM;
+    float2 *tw = smem;
+    build_twiddles<M>(tw);
+    float2 *buf = smem + P<M>::TW_WORDS + p * PLEN;
+    __syncthreads();
+    const int npairs = (nrows + 1) / 2;
+    for (int pair0 = blockIdx.x * teams; pair0 < npairs; pair0 += gridDim.x * teams) {
+        const int ra = 2 * (pair0 + p), rb = ra + 1;
+        const bool ha = ra < nrows, hb = rb < nrows;
+        first_pass_load<true, M>(buf, [&](int n) {
+            const int k = n <= HALF ? n : M - n;
+            float2 a = ha ? __ldg(in + lay.at(ra, k)) : make_float2(0.f, 0.f);
+            float2 b = hb ? __ldg(in + lay.at(rb, k)) : make_float2(0.f, 0.f);
+            if (k == 0 || k == HALF) {  // c2r uses only the real part of the DC and Nyquist bins
+                a.y = 0.0f;
+                b.y = 0.0f;
+            }
+            return n <= HALF ? make_float2(a.x - b.y, a.y + b.x)   // Xa + i Xb
+                             : make_float2(a.x + b.y, b.x - a.y);  // conj(Xa) + i conj(Xb)
+        }, t);
+        passes<true, M, 1, NP - 1>(buf, tw, t);
+        last_pass_store<true, M>(buf, tw, [&](int n, float2 z) {
+            int j = n - shift;
+            if (j < 0) j += M;
+            if (j < out_cols) {
+                if (ha) out[(size_t)ra * out_cols + j] = __fdiv_rn(z.x, div);
+                if (hb) out[(size_t)rb * out_cols + j] = __fdiv_rn(z.y, div);
+            }
+        }, t);
+        __syncthreads();
+    }
+}
+
 // --------------------------------------------------------------------------
 // 3. Row C2R of Hermitian half-rows [2q, 2q+1]; output column j takes sample
 //    (j + shift) mod M, divided by `div` (M^2).
@@ -427,6 +609,15 @@ int row_teams(size_t per_team, size_t fixed) {
 template <int M, class OutL>
 int launch_rfft_rows(const float *x, int nrows, int ncols, int col_off, float2 *out, OutL lay, cudaStream_t st) {
     const size_t tw = P<M>::TW_WORDS * sizeof(float2), seq = P<M>::PLEN * sizeof(float2);
+    if constexpr (direct_ok<M>()) {
+        const int teams = row_teams<M>(seq, tw);
+        const size_t smem = tw + (size_t)teams * seq;
+        const int threads = teams * P<M>::TEAM;
+        const int items = ((nrows + 1) / 2 + teams - 1) / teams;
+        const int grid = persistent_grid(rfft_rows_direct<M, OutL>, threads, smem, items);
+        rfft_rows_direct<M, OutL><<<grid, threads, smem, st>>>(x, nrows, ncols, col_off, out, lay);
+        return check_launch("rfft_rows");
+    }
     const bool db = tw + 2 * seq <= kMaxSmem;
     const int teams = row_teams<M>((db ? 2 : 1) * seq, tw);
     const size_t smem = tw + (size_t)teams * (db ? 2 : 1) * seq;
@@ -446,6 +637,15 @@ template <int M, class InL>
 int launch_irfft_rows(const float2 *in, InL lay, int nrows, float *out, int out_cols, int shift, float div,
                       cudaStream_t st) {
     const size_t tw = P<M>::TW_WORDS * sizeof(float2), seq = P<M>::PLEN * sizeof(float2);
+    if constexpr (direct_ok<M>()) {
+        const int teams = row_teams<M>(seq, tw);
+        const size_t smem = tw + (size_t)teams * seq;
+        const int threads = teams * P<M>::TEAM;
+        const int items = ((nrows + 1) / 2 + teams - 1) / teams;
+        const int grid = persistent_grid(irfft_rows_direct<M, InL>, threads, smem, items);
+        irfft_rows_direct<M, InL><<<grid, threads, smem, st>>>(in, lay, nrows, out, out_cols, shift, div);
+        return check_launch("irfft_rows");
+    }
     const size_t stage = (size_t)((2 * (M / 2 + 1) + 1) & ~1) * sizeof(float2);
     const bool db = tw + seq + 2 * stage <= 112 * 1024;
     const size_t per_team = seq + (db ? 2 : 1) * stage;
@@ -470,6 +670,13 @@ int launch_cols(const float2 *in, InL in_lay, int in_rows, int in_off, const flo
     constexpr bool FUSED = MODE == kConv && P<M>::plan.fusable;
     const size_t tw = P<M>::TW_WORDS * sizeof(float2), set = (size_t)C * P<M>::PLEN * sizeof(float2);
     const int threads = C * P<M>::TEAM;
+    if constexpr (FUSED && direct_ok<M>()) {
+        const size_t smem = tw + set;
+        const int grid = persistent_grid(conv_cols_direct<M, InL, OutL>, threads, smem, P<M>::plan.groups);
+        conv_cols_direct<M, InL, OutL><<<grid, threads, smem, st>>>(in, in_lay, in_rows, in_off, h, out, out_lay,
+                                                                     out_rows, shift);
+        return check_launch("conv_cols");
+    }
     const bool db = tw + 2 * set <= kMaxSmem;
     const size_t smem = tw + (db ? 2 : 1) * set;
     if (db) {
