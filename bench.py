@@ -134,10 +134,15 @@ def iuwt_algorithmic_bytes(n, s):
 
 
 def iuwt_kernel_bytes(n, s):
-    # Compulsory bytes of the 3 s atrous_band launches of one step: per scale the
-    # decomposition's smoothing (read 1 plane, write 1), its detail pass (read 2,
-    # write 1) and the recomposition's smoothing + add (read 2, write 1).
-    return 4 * n * n * s * (2 + 3 + 3)
+    """Compulsory bytes of the 2s + 1 passes of one step, plane by plane (4 n^2 bytes each).
+
+    Decomposition: the first smoothing (read 1 plane, write 1), s - 1 fused
+    detail + next-smoothing passes (read the smoothed plane and its
+    predecessor, write the detail and the next smoothed plane: 4), the last
+    detail pass (read 2, write 1). Recomposition from the smoothed plane: s
+    smoothing + add passes (read 2, write 1).
+    """
+    return 4 * n * n * ((2 + 4 * (s - 1) + 3) + 3 * s)
 
 
 def measure_iuwt(steps, warmup, seed=0):

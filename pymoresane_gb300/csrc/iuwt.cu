@@ -146,6 +146,61 @@ atrous_band(const float *__restrict__ in, float *__restrict__ out, const float *
     }
 }
 
+// Fused decomposition step: one launch reads the smoothed plane C once and
+// writes both the detail of scale s, w = (C0 - h_s * C) [* mask], and the next
+// smoothing C' = h_{s+1} * C. The vertical taps of the two dilations d and 2d
+// share the rows r +- 2d (seven row loads instead of ten); the two vertical
+// results stay in shared memory and both horizontal passes and epilogues run
+// from there. The arithmetic of each output is that of its own atrous_band
+// pass, so the results are bit-identical to the unfused sequence.
+// c0 may alias next: each element of c0 is read once, by the thread that
+// writes next at the same index, before it writes (no __restrict__, no __ldg).
+template <bool MASK>
+__global__ void __launch_bounds__(kThreads)
+atrous_pair(const float *__restrict__ in, const float *c0, const float *__restrict__ mask, float *__restrict__ w,
+            float *next, int ny, int nx, int d) {
+    extern __shared__ float4 smem4[];
+    const int r = blockIdx.x;
+    const int nx4 = nx >> 2;
+    const int nt = blockDim.x;
+    const float4 *in4 = reinterpret_cast<const float4 *>(in);
+    const size_t rc = (size_t)r * nx4, rm2 = (size_t)mirror(r - 2 * d, ny) * nx4,
+                 rm1 = (size_t)mirror(r - d, ny) * nx4, rp1 = (size_t)mirror(r + d, ny) * nx4,
+                 rp2 = (size_t)mirror(r + 2 * d, ny) * nx4, rm4 = (size_t)mirror(r - 4 * d, ny) * nx4,
+                 rp4 = (size_t)mirror(r + 4 * d, ny) * nx4;
+    for (int c4 = threadIdx.x; c4 < nx4; c4 += nt) {
+        const float4 c = __ldg(in4 + rc + c4), a = __ldg(in4 + rm2 + c4), b = __ldg(in4 + rm1 + c4),
+                     e = __ldg(in4 + rp1 + c4), f = __ldg(in4 + rp2 + c4), a2 = __ldg(in4 + rm4 + c4),
+                     f2 = __ldg(in4 + rp4 + c4);
+        smem4[c4] = b3_tap4(c, a, b, e, f);            // dilation d
+        smem4[nx4 + c4] = b3_tap4(c, a2, a, f, f2);    // dilation 2d: taps r -+ 4d, r -+ 2d
+    }
+    __syncthreads();
+    const float *band1 = reinterpret_cast<const float *>(smem4);
+    const float *band2 = band1 + nx;
+    const float4 *c04 = reinterpret_cast<const float4 *>(c0);
+    float4 *w4 = reinterpret_cast<float4 *>(w);
+    float4 *next4 = reinterpret_cast<float4 *>(next);
+    for (int c4 = threadIdx.x; c4 < nx4; c4 += nt) {
+        const size_t g4 = rc + c4;
+        const float4 x = c04[g4];
+        float4 v = horizontal4(band1, c4 * 4, nx, d);
+        v.x = __fsub_rn(x.x, v.x);
+        v.y = __fsub_rn(x.y, v.y);
+        v.z = __fsub_rn(x.z, v.z);
+        v.w = __fsub_rn(x.w, v.w);
+        if (MASK) {  // mask * detail, as the reference's separate product (main.py:383)
+            const float4 mk = __ldg(reinterpret_cast<const float4 *>(mask) + g4);
+            v.x = __fmul_rn(v.x, mk.x);
+            v.y = __fmul_rn(v.y, mk.y);
+            v.z = __fmul_rn(v.z, mk.z);
+            v.w = __fmul_rn(v.w, mk.w);
+        }
+        w4[g4] = v;
+        next4[g4] = horizontal4(band2, c4 * 4, nx, 2 * d);
+    }
+}
+
 // rec = 0 + w: the first recomposition step when no smoothed plane is given
 // (the smoothing of an all-zero plane is exactly +0, and +0 + w maps -0 to +0
 // exactly as the reference's addition does).
@@ -181,6 +236,22 @@ int launch_band(const float *in, float *out, const float *aux, int ny, int nx, i
     const int threads = work4 >= kThreads ? kThreads : ((work4 + 31) / 32) * 32;
     atrous_band<EPI><<<grid, threads, smem, st>>>(in, out, aux, mask, ny, nx, d, band);
     return check_launch("atrous_band");
+}
+
+// The fused step keeps two rows in shared memory.
+bool pair_fits(int nx) { return (size_t)2 * nx * sizeof(float) <= (size_t)kMaxSmem; }
+
+template <bool MASK>
+int launch_pair(const float *in, const float *c0, const float *mask, float *w, float *next, int ny, int nx, int d,
+                cudaStream_t st) {
+    static std::once_flag once;
+    std::call_once(once, [] {
+        cudaFuncSetAttribute(atrous_pair<MASK>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxSmem);
+    });
+    const int nx4 = nx >> 2;
+    const int threads = nx4 >= kThreads ? kThreads : ((nx4 + 31) / 32) * 32;
+    atrous_pair<MASK><<<ny, threads, 2 * (size_t)nx * sizeof(float), st>>>(in, c0, mask, w, next, ny, nx, d);
+    return check_launch("atrous_pair");
 }
 
 int launch_zero_plus(const float *w, float *out, size_t n, cudaStream_t st) {
@@ -227,8 +298,10 @@ int iuwt_smooth_detail_mask(const float *in, const float *c0, const float *mask,
     return launch_band<kDetailMask>(in, w, c0, ny, nx, 1 << scale, st, mask);
 }
 
-int iuwt_decompose_impl(const float *d_in, float *d_detail, float *d_smoothed, int ny, int nx, int scale_count,
-                        int scale_adjust, float *p0, float *p1, cudaStream_t st, const float *d_mask = nullptr) {
+// Decomposition as the reference sequences it: per scale one smoothing and one
+// detail pass (used for a single detail plane or rows too long for atrous_pair).
+int iuwt_decompose_unfused(const float *d_in, float *d_detail, float *d_smoothed, int ny, int nx, int scale_count,
+                           int scale_adjust, float *p0, float *p1, cudaStream_t st, const float *d_mask) {
     const size_t plane = (size_t)ny * nx;
     float *bufs[2] = {p0, p1};
     const float *cur = d_in;
@@ -257,6 +330,49 @@ int iuwt_decompose_impl(const float *d_in, float *d_detail, float *d_smoothed, i
         MSN_TRY(check_cuda(cudaMemcpyAsync(d_smoothed, cur, plane * sizeof(float), cudaMemcpyDeviceToDevice, st),
                            "copy smoothed plane"));
     }
+    return MSN_OK;
+}
+
+// Decomposition with the detail pass of scale s fused with the smoothing of
+// scale s + 1 (atrous_pair): scale_count - scale_adjust + 1 launches after the
+// warm-up smoothings instead of twice that. Scratch: the two planes p0, p1.
+int iuwt_decompose_impl(const float *d_in, float *d_detail, float *d_smoothed, int ny, int nx, int scale_count,
+                        int scale_adjust, float *p0, float *p1, cudaStream_t st, const float *d_mask = nullptr) {
+    if (scale_count - scale_adjust < 2 || !pair_fits(nx))
+        return iuwt_decompose_unfused(d_in, d_detail, d_smoothed, ny, nx, scale_count, scale_adjust, p0, p1, st,
+                                      d_mask);
+    const size_t plane = (size_t)ny * nx;
+    float *bufs[2] = {p0, p1};
+    const float *cur = d_in;  // C_{s-1}: the detail epilogue's minuend
+    int cur_buf = -1;
+    for (int s = 0; s < scale_adjust; ++s) {
+        const int nb = cur_buf == 0 ? 1 : 0;
+        MSN_TRY(iuwt_smooth(cur, bufs[nb], ny, nx, s, st));
+        cur = bufs[nb];
+        cur_buf = nb;
+    }
+    int c_buf = cur_buf == 0 ? 1 : 0;
+    float *c = bufs[c_buf];  // C_s = h_s * C_{s-1}
+    MSN_TRY(iuwt_smooth(cur, c, ny, nx, scale_adjust, st));
+    for (int s = scale_adjust; s < scale_count - 1; ++s) {
+        float *w = d_detail + (size_t)(s - scale_adjust) * plane;
+        // C_{s+1} overwrites C_{s-1} (or fills the free plane / the caller's smoothed plane)
+        float *next = (s == scale_count - 2 && d_smoothed) ? d_smoothed : bufs[1 - c_buf];
+        if (d_mask)
+            MSN_TRY(launch_pair<true>(c, cur, d_mask + (size_t)(s - scale_adjust) * plane, w, next, ny, nx, 1 << s,
+                                      st));
+        else
+            MSN_TRY(launch_pair<false>(c, cur, nullptr, w, next, ny, nx, 1 << s, st));
+        cur = c;
+        c = next;
+        c_buf = (next == d_smoothed) ? -1 : 1 - c_buf;
+    }
+    const int s = scale_count - 1;
+    float *w = d_detail + (size_t)(s - scale_adjust) * plane;
+    if (d_mask)
+        MSN_TRY(iuwt_smooth_detail_mask(c, cur, d_mask + (size_t)(s - scale_adjust) * plane, w, ny, nx, s, st));
+    else
+        MSN_TRY(iuwt_smooth_detail(c, cur, w, ny, nx, s, st));
     return MSN_OK;
 }
 
