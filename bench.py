@@ -264,6 +264,10 @@ def run_deconv(args, rank, world, dist):
 
     def step():
         eng = Deconvolver(psf)
+        if args.driver == "host":
+            # the same kernels driven step by step from the host (no CUDA graphs): ncu can
+            # profile every launch this way, it cannot inside graphs with conditional nodes
+            eng.native_major_loop = eng.native_minor_loop = False
         model, residual, major = eng.moresane(dirty, **DECONV_KW)
         return eng, model, residual
 
@@ -462,6 +466,8 @@ def main():
     ap.add_argument("--rate", type=float, default=40.0, help="serve workload: arrivals per second")
     ap.add_argument("--distinct", type=int, default=3, help="batch / serve: distinct problems per size")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--driver", default="native", choices=["native", "host"],
+                    help="deconv: native = minor/major loops in libmsn (graphs); host = step by step (for ncu)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -610,7 +616,7 @@ def main():
             "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": "moresane_2048x2048_psf4096_S7_linear (BASELINE config 2)",
-                       "trajectory_major_minor": list(res["traj"]),
+                       "trajectory_major_minor": list(res["traj"]), "driver": args.driver,
                        "l2": "working set > 0.6 GB per deconvolution > 129 MB L2 (no flush needed)",
                        "parallelism": f"replicas x{world}"},
             "latency_ms": {"p50": percentile(res["lat"], 50), "p99": percentile(res["lat"], 99),

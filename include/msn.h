@@ -225,6 +225,18 @@ int msn_snr_update(const float *d_e, float *d_ms, const float *d_q, const double
 
 /* alpha = scal[0] / scal[1] -> scal[2]; xn = x + alpha p; *d_neg_count = #(xn < 0)
  * (pymoresane/main.py:386-390). */
+/* Segment activity of a mask: d_flags[s] = 1 when any of the 128 floats
+ * [128 s, 128 s + 128) of d_mask [n] is non-zero; msn_segment_flags_bytes(n)
+ * bytes. No counterpart in the reference (support of the sparse SNR pass). */
+size_t msn_segment_flags_bytes(size_t n);
+int msn_segment_flags(const float *d_mask, size_t n, unsigned char *d_flags, void *stream);
+
+/* msn_snr_update restricted to the segments flagged by msn_segment_flags of the
+ * extraction mask (zero elsewhere in all three stacks); bit-identical result. */
+int msn_snr_update_masked(const float *d_e, float *d_ms, const float *d_q, const double *d_scal, size_t n,
+                          const unsigned char *d_flags, double *d_out2, void *d_work, size_t work_bytes,
+                          void *stream);
+
 int msn_cg_alpha_x(const float *d_x, const float *d_p, double *d_scal, float *d_xn, size_t n, int *d_neg_count,
                    void *stream);
 
@@ -292,6 +304,7 @@ typedef struct msn_minor_args {
     double *scal;           /* 5 doubles: r.r, p.Ap, alpha, rn.rn, beta */
     double *snr2;           /* 2 doubles: |esrc|^2, |esrc - ms|^2 */
     int *neg;               /* 1 int: #(xn < 0) */
+    unsigned char *seg_flags; /* msn_segment_flags_bytes(planes * n * n) */
     void *fft_work;         /* msn_fft_workspace_bytes(n, m) */
     size_t fft_work_bytes;
     void *iuwt_work;        /* msn_iuwt_workspace_bytes(n, n) */
@@ -384,6 +397,7 @@ typedef struct msn_moresane_args {
     double *snr2;            /* 2 */
     double *std4;            /* 4 */
     int *neg;                /* 1 */
+    unsigned char *seg_flags; /* msn_segment_flags_bytes(scale_count * ns * ns) */
     float *fmax;             /* 1 */
     void *small;             /* >= 16 and >= 4 * scale_count bytes */
     size_t small_bytes;

@@ -108,12 +108,19 @@ finalize_pairs(const double *__restrict__ partials, double *__restrict__ out) {
 // mask * W(H p) is the plane stack Q already formed for Ap, so the model sources of
 // pymoresane/main.py:413-416 and the norms of snr_ratio (iuwt_toolbox.py:304) come
 // from one pass instead of a convolution plus a decomposition.
+// With seg_flags, 32-float4 segments whose flag is 0 are skipped: there e, q
+// and ms are all zero (the extraction mask is zero), so each skipped term would
+// add exactly +0 to the same per-thread partial, and the sums are bit-identical
+// to the dense pass. A warp's 32 consecutive indices form one segment, so the
+// test is warp-uniform.
 __global__ void __launch_bounds__(kRedThreads)
 snr_update(const float4 *__restrict__ e, float4 *__restrict__ ms, const float4 *__restrict__ q,
-           const double *__restrict__ scal, size_t n4, double *__restrict__ partials) {
+           const double *__restrict__ scal, size_t n4, double *__restrict__ partials,
+           const unsigned char *__restrict__ seg_flags) {
     const float a = (float)scal[S_ALPHA];
     double s0 = 0.0, s1 = 0.0;
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n4; i += (size_t)gridDim.x * blockDim.x) {
+        if (seg_flags && seg_flags[i >> 5] == 0) continue;
         const float4 ev = __ldg(e + i), qv = __ldg(q + i);
         float4 mv = ms[i];
         mv.x = __fadd_rn(mv.x, __fmul_rn(a, qv.x));
@@ -191,6 +198,24 @@ cg_residual(const float4 *__restrict__ r, const float4 *__restrict__ ap, const d
     if (threadIdx.x == 0) {
         partials[2 * blockIdx.x] = s;
         partials[2 * blockIdx.x + 1] = 0.0;
+    }
+}
+
+// flags[s] = 1 when any element of float4 segment s (32 float4) of m is non-zero.
+__global__ void segment_flags(const float4 *__restrict__ m, size_t n4, unsigned char *__restrict__ flags) {
+    const size_t nseg = (n4 + 31) / 32;
+    const int lane = threadIdx.x & 31;
+    const size_t warp = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const size_t nwarps = ((size_t)gridDim.x * blockDim.x) >> 5;
+    for (size_t seg = warp; seg < nseg; seg += nwarps) {
+        const size_t i = seg * 32 + lane;
+        bool nz = false;
+        if (i < n4) {
+            const float4 v = __ldg(m + i);
+            nz = v.x != 0.0f || v.y != 0.0f || v.z != 0.0f || v.w != 0.0f;
+        }
+        const unsigned any = __any_sync(0xffffffffu, nz);
+        if (lane == 0) flags[seg] = any ? 1 : 0;
     }
 }
 
@@ -339,7 +364,40 @@ extern "C" int msn_snr_update(const float *d_e, float *d_ms, const float *d_q, c
     cudaStream_t st = as_stream(stream);
     double *partials = (double *)d_work;
     snr_update<<<kRedGrid, kRedThreads, 0, st>>>((const float4 *)d_e, (float4 *)d_ms, (const float4 *)d_q, d_scal, n / 4,
-                                                  partials);
+                                                  partials, nullptr);
+    MSN_TRY(check_launch("snr_update"));
+    finalize_pairs<<<1, kFinalizeThreads, 0, st>>>(partials, d_out2);
+    return check_launch("finalize_pairs");
+}
+
+extern "C" size_t msn_segment_flags_bytes(size_t n) { return (n / 4 + 31) / 32; }
+
+extern "C" int msn_segment_flags(const float *d_mask, size_t n, unsigned char *d_flags, void *stream) {
+    clear_error();
+    if (!d_mask || !d_flags) return set_error(MSN_ERR_INVALID, "msn_segment_flags: null pointer");
+    if (n % 4 || !aligned16(d_mask))
+        return set_error(MSN_ERR_INVALID, "msn_segment_flags: length must be a multiple of 4, pointer 16-byte aligned");
+    const size_t nseg = (n / 4 + 31) / 32;
+    size_t g = (nseg * 32 + 255) / 256;
+    if (g > 152 * 8) g = 152 * 8;
+    segment_flags<<<(int)(g < 1 ? 1 : g), 256, 0, as_stream(stream)>>>((const float4 *)d_mask, n / 4, d_flags);
+    return check_launch("segment_flags");
+}
+
+extern "C" int msn_snr_update_masked(const float *d_e, float *d_ms, const float *d_q, const double *d_scal, size_t n,
+                                     const unsigned char *d_flags, double *d_out2, void *d_work, size_t work_bytes,
+                                     void *stream) {
+    clear_error();
+    if (!d_e || !d_ms || !d_q || !d_scal || !d_out2 || !d_flags)
+        return set_error(MSN_ERR_INVALID, "msn_snr_update_masked: null pointer");
+    if (n % 4 || !aligned16(d_e) || !aligned16(d_ms) || !aligned16(d_q))
+        return set_error(MSN_ERR_INVALID,
+                         "msn_snr_update_masked: length must be a multiple of 4, pointers 16-byte aligned");
+    MSN_TRY(check_red_ws(d_work, work_bytes, "msn_snr_update_masked"));
+    cudaStream_t st = as_stream(stream);
+    double *partials = (double *)d_work;
+    snr_update<<<kRedGrid, kRedThreads, 0, st>>>((const float4 *)d_e, (float4 *)d_ms, (const float4 *)d_q, d_scal, n / 4,
+                                                  partials, d_flags);
     MSN_TRY(check_launch("snr_update"));
     finalize_pairs<<<1, kFinalizeThreads, 0, st>>>(partials, d_out2);
     return check_launch("finalize_pairs");

@@ -176,6 +176,7 @@ msn_minor_args make_key(const msn_minor_args *a) {
     k.scal = a->scal;
     k.snr2 = a->snr2;
     k.neg = a->neg;
+    k.seg_flags = a->seg_flags;
     k.fft_work = a->fft_work;
     k.fft_work_bytes = a->fft_work_bytes;
     k.iuwt_work = a->iuwt_work;
@@ -251,6 +252,8 @@ int build_graph(Engine *e, const msn_minor_args *a, CacheEntry *ce) {
         MSN_TRY(check_cuda(cudaMemsetAsync(a->ms, 0, (size_t)planes * nvec * sizeof(float), st), "zero sources"));
         MSN_TRY(check_cuda(cudaMemcpyAsync(a->r, a->rec, nvec * sizeof(float), cudaMemcpyDeviceToDevice, st), "r"));
         MSN_TRY(check_cuda(cudaMemcpyAsync(a->p, a->rec, nvec * sizeof(float), cudaMemcpyDeviceToDevice, st), "p"));
+        // the extraction mask is fixed for the whole minor loop: flag its non-empty segments once
+        MSN_TRY(msn_segment_flags(a->emask, (size_t)planes * nvec, a->seg_flags, st));
         minor_init<<<1, 1, 0, st>>>(state, a->minor_loop_miter);
         MSN_TRY(check_launch("minor_init"));
         return add_conditional(st, while_h, cudaGraphCondTypeWhile, &body);
@@ -274,8 +277,8 @@ int build_graph(Engine *e, const msn_minor_args *a, CacheEntry *ce) {
                 return apply_a(a, a->p, a->ap, bst);
             }));
         }
-        MSN_TRY(msn_snr_update(a->esrc, a->ms, a->planes, a->scal, (size_t)planes * nvec, a->snr2, a->red_work,
-                               a->red_work_bytes, st));
+        MSN_TRY(msn_snr_update_masked(a->esrc, a->ms, a->planes, a->scal, (size_t)planes * nvec, a->seg_flags,
+                                      a->snr2, a->red_work, a->red_work_bytes, st));
         minor_control<<<1, 1, 0, st>>>(state, a->snr2, hist, kHistory, while_h);
         MSN_TRY(check_launch("minor_control"));
         MSN_TRY(msn_cg_residual(a->r, a->ap, a->scal, a->rn, nvec, a->red_work, a->red_work_bytes, st));
@@ -310,7 +313,7 @@ int validate_args(const msn_minor_args *a) {
     if (a->minor_loop_miter < 0) return set_error(MSN_ERR_INVALID, "%s: negative minor_loop_miter", fn);
     const void *ptrs[] = {a->spec, a->rec, a->x,     a->xn,   a->r,    a->rn,  a->p,        a->ap,
                           a->tmp,  a->planes, a->emask, a->esrc, a->ms, a->scal, a->snr2, a->neg,
-                          a->fft_work, a->iuwt_work, a->red_work};
+                          a->seg_flags, a->fft_work, a->iuwt_work, a->red_work};
     for (const void *p : ptrs)
         if (p == nullptr) return set_error(MSN_ERR_INVALID, "%s: null buffer in the argument block", fn);
     const void *vecs[] = {a->rec, a->x, a->xn, a->r, a->rn, a->p, a->ap, a->tmp, a->planes, a->emask, a->esrc, a->ms};
@@ -476,7 +479,7 @@ int validate_run(const msn_moresane_args *a) {
     const void *ptrs[] = {a->dirty, a->energies, a->spec_sub, a->spec_data, a->model, a->residual, a->dec, a->thr,
                           a->emask, a->esrc, a->planes, a->ms, a->x, a->xn, a->r, a->rn, a->p, a->ap, a->tmp,
                           a->rec, a->masked, a->sub, a->conv_full, a->sigma, a->pmax, a->scal, a->snr2, a->std4,
-                          a->neg, a->fmax, a->small, a->iuwt_work, a->fft_work, a->fft_work_full, a->tool_work,
+                          a->neg, a->seg_flags, a->fmax, a->small, a->iuwt_work, a->fft_work, a->fft_work_full, a->tool_work,
                           a->red_work};
     for (const void *p : ptrs)
         if (!p) return set_error(MSN_ERR_INVALID, "%s: null buffer in the argument block", fn);
@@ -549,6 +552,7 @@ int run_moresane(Engine *e, const msn_moresane_args *a, msn_moresane_result *res
     m.scal = a->scal;
     m.snr2 = a->snr2;
     m.neg = a->neg;
+    m.seg_flags = a->seg_flags;
     m.fft_work = a->fft_work;
     m.fft_work_bytes = a->fft_work_bytes;
     m.iuwt_work = a->iuwt_work;

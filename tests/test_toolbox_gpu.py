@@ -192,3 +192,44 @@ def test_region_std_and_model_update(cuda):
     m = np.zeros((96, 96), np.float32)
     m[16:80, 16:80] += np.float32(0.2) * x
     assert np.array_equal(model.cpu().numpy(), m)
+
+
+@pytest.mark.parametrize("planes,n,blobs", [(3, 64, 2), (5, 256, 6), (2, 100, 0), (7, 512, 40)])
+def test_snr_update_masked_matches_dense(cuda, planes, n, blobs):
+    """The segment-skipping SNR pass gives the dense pass's running sum and norms bit for bit."""
+    from pymoresane_gb300 import _native
+    rng = np.random.default_rng(planes * n + blobs)
+    mask = np.zeros((planes, n, n), np.float32)
+    for _ in range(blobs):
+        p, y, x = rng.integers(0, planes), rng.integers(0, n - 8), rng.integers(0, n - 8)
+        mask[p, y:y + rng.integers(1, 8), x:x + rng.integers(1, 8)] = 1.0
+    w = rng.standard_normal(mask.shape).astype(np.float32)
+    e = torch.from_numpy(mask * w).cuda()                     # extracted sources (signed zeros outside)
+    q = torch.from_numpy(mask * rng.standard_normal(mask.shape).astype(np.float32)).cuda()
+    ms0 = torch.from_numpy(mask * rng.standard_normal(mask.shape).astype(np.float32)).cuda()
+    scal = torch.tensor([1.0, 2.0, -0.37, 0.0, 0.0, 0, 0, 0], dtype=torch.float64, device="cuda")
+    work = dev.reduce_workspace(e.device)
+    st = dev.stream_handle()
+    n_el = e.numel()
+    flags = torch.empty(max(1, _native.query("msn_segment_flags_bytes", n_el)), dtype=torch.uint8, device="cuda")
+    _native.call("msn_segment_flags", torch.from_numpy(mask).cuda().data_ptr(), n_el, flags.data_ptr(), st)
+    seg = mask.reshape(-1)
+    pad = (-seg.size) % 128
+    want = (np.concatenate([seg, np.zeros(pad, np.float32)]).reshape(-1, 128) != 0).any(axis=1)
+    assert np.array_equal(flags.cpu().numpy()[:want.size].astype(bool), want)
+    outs = []
+    for masked in (False, True):
+        ms = ms0.clone()
+        out2 = torch.zeros(2, dtype=torch.float64, device="cuda")
+        if masked:
+            _native.call("msn_snr_update_masked", e.data_ptr(), ms.data_ptr(), q.data_ptr(), scal.data_ptr(), n_el,
+                         flags.data_ptr(), out2.data_ptr(), work.data_ptr(), work.numel(), st)
+        else:
+            _native.call("msn_snr_update", e.data_ptr(), ms.data_ptr(), q.data_ptr(), scal.data_ptr(), n_el,
+                         out2.data_ptr(), work.data_ptr(), work.numel(), st)
+        outs.append((ms.cpu().numpy(), out2.cpu().numpy()))
+    assert np.array_equal(outs[0][0], outs[1][0])
+    assert np.array_equal(outs[0][1], outs[1][1])
+    # and the running sum is ms + (float32)alpha * q as in the reference's float32 update
+    a = np.float32(-0.37)
+    assert np.array_equal(outs[1][0], ms0.cpu().numpy() + a * q.cpu().numpy())
