@@ -73,6 +73,15 @@ int msn_iuwt_decompose(const float *d_in, float *d_detail, float *d_smoothed, in
 int msn_iuwt_decompose_masked(const float *d_in, const float *d_mask, float *d_detail, int ny, int nx,
                               int scale_count, int scale_adjust, void *d_work, size_t work_bytes, void *stream);
 
+/* msn_iuwt_decompose_masked for a mask with empty rows: d_row_flags
+ * [planes][ny] (msn_row_flags of the mask) is 0 where a mask row is all zero,
+ * and those detail rows are NOT written -- the caller keeps them zero (the
+ * values there would be zeros). No counterpart in the reference: the minor
+ * loop's A operator with a sparse extraction mask (main.py:375-384). */
+int msn_iuwt_decompose_masked_rows(const float *d_in, const float *d_mask, const unsigned char *d_row_flags,
+                                   float *d_detail, int ny, int nx, int scale_count, int scale_adjust, void *d_work,
+                                   size_t work_bytes, void *stream);
+
 /* Replaces iuwt_recomposition(in1, scale_adjust, mode='gpu',
  * smoothed_array=...) -- pymoresane/iuwt.py:43 -> gpu_iuwt_recomposition
  * pymoresane/iuwt.py:501-581.
@@ -231,6 +240,9 @@ int msn_snr_update(const float *d_e, float *d_ms, const float *d_q, const double
 size_t msn_segment_flags_bytes(size_t n);
 int msn_segment_flags(const float *d_mask, size_t n, unsigned char *d_flags, void *stream);
 
+/* d_flags[r] = 1 when row r of d_mask [rows][cols] has a non-zero element. */
+int msn_row_flags(const float *d_mask, size_t rows, int cols, unsigned char *d_flags, void *stream);
+
 /* msn_snr_update restricted to the segments flagged by msn_segment_flags of the
  * extraction mask (zero elsewhere in all three stacks); bit-identical result. */
 int msn_snr_update_masked(const float *d_e, float *d_ms, const float *d_q, const double *d_scal, size_t n,
@@ -305,6 +317,7 @@ typedef struct msn_minor_args {
     double *snr2;           /* 2 doubles: |esrc|^2, |esrc - ms|^2 */
     int *neg;               /* 1 int: #(xn < 0) */
     unsigned char *seg_flags; /* msn_segment_flags_bytes(planes * n * n) */
+    unsigned char *row_flags; /* planes * n bytes */
     void *fft_work;         /* msn_fft_workspace_bytes(n, m) */
     size_t fft_work_bytes;
     void *iuwt_work;        /* msn_iuwt_workspace_bytes(n, n) */
@@ -398,6 +411,7 @@ typedef struct msn_moresane_args {
     double *std4;            /* 4 */
     int *neg;                /* 1 */
     unsigned char *seg_flags; /* msn_segment_flags_bytes(scale_count * ns * ns) */
+    unsigned char *row_flags; /* scale_count * ns bytes */
     float *fmax;             /* 1 */
     void *small;             /* >= 16 and >= 4 * scale_count bytes */
     size_t small_bytes;

@@ -219,6 +219,22 @@ __global__ void segment_flags(const float4 *__restrict__ m, size_t n4, unsigned 
     }
 }
 
+// flags[r] = 1 when row r (cols floats, cols % 4 == 0) of m has a non-zero element.
+__global__ void row_flags(const float4 *__restrict__ m, size_t rows, int cols4, unsigned char *__restrict__ flags) {
+    const int lane = threadIdx.x & 31;
+    const size_t warp = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const size_t nwarps = ((size_t)gridDim.x * blockDim.x) >> 5;
+    for (size_t r = warp; r < rows; r += nwarps) {
+        bool nz = false;
+        for (int c = lane; c < cols4; c += 32) {
+            const float4 v = __ldg(m + r * cols4 + c);
+            nz = nz || v.x != 0.0f || v.y != 0.0f || v.z != 0.0f || v.w != 0.0f;
+        }
+        const unsigned any = __any_sync(0xffffffffu, nz);
+        if (lane == 0) flags[r] = any ? 1 : 0;
+    }
+}
+
 __global__ void cg_beta(double *__restrict__ scal) {
     // beta = rn.rn / r.r (main.py:407-409); S_RNRN was written by finalize_pairs.
     scal[S_BETA] = scal[S_RNRN] / scal[S_RR];
@@ -382,6 +398,17 @@ extern "C" int msn_segment_flags(const float *d_mask, size_t n, unsigned char *d
     if (g > 152 * 8) g = 152 * 8;
     segment_flags<<<(int)(g < 1 ? 1 : g), 256, 0, as_stream(stream)>>>((const float4 *)d_mask, n / 4, d_flags);
     return check_launch("segment_flags");
+}
+
+extern "C" int msn_row_flags(const float *d_mask, size_t rows, int cols, unsigned char *d_flags, void *stream) {
+    clear_error();
+    if (!d_mask || !d_flags) return set_error(MSN_ERR_INVALID, "msn_row_flags: null pointer");
+    if (cols <= 0 || cols % 4 || !aligned16(d_mask))
+        return set_error(MSN_ERR_INVALID, "msn_row_flags: cols must be a positive multiple of 4, pointer 16-byte aligned");
+    size_t g = (rows * 32 + 255) / 256;
+    if (g > 152 * 8) g = 152 * 8;
+    row_flags<<<(int)(g < 1 ? 1 : g), 256, 0, as_stream(stream)>>>((const float4 *)d_mask, rows, cols / 4, d_flags);
+    return check_launch("row_flags");
 }
 
 extern "C" int msn_snr_update_masked(const float *d_e, float *d_ms, const float *d_q, const double *d_scal, size_t n,

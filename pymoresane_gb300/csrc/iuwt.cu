@@ -86,8 +86,11 @@ __device__ __forceinline__ float4 horizontal4(const float *__restrict__ s, int c
 template <int EPI>
 __global__ void __launch_bounds__(kThreads)
 atrous_band(const float *__restrict__ in, float *__restrict__ out, const float *__restrict__ aux,
-            const float *__restrict__ mask, int ny, int nx, int d, int band_rows) {
+            const float *__restrict__ mask, int ny, int nx, int d, int band_rows,
+            const unsigned char *__restrict__ row_flags) {
     extern __shared__ float4 smem4[];
+    // masked detail with row flags: rows whose mask row is empty are left as they are (zero)
+    if (EPI == kDetailMask && row_flags && band_rows == 1 && !row_flags[blockIdx.x]) return;
     const float *band = reinterpret_cast<const float *>(smem4);
     const int r0 = blockIdx.x * band_rows;
     const int rows = min(band_rows, ny - r0);
@@ -158,9 +161,11 @@ atrous_band(const float *__restrict__ in, float *__restrict__ out, const float *
 template <bool MASK>
 __global__ void __launch_bounds__(kThreads)
 atrous_pair(const float *__restrict__ in, const float *c0, const float *__restrict__ mask, float *__restrict__ w,
-            float *next, int ny, int nx, int d) {
+            float *next, int ny, int nx, int d, const unsigned char *__restrict__ row_flags) {
     extern __shared__ float4 smem4[];
     const int r = blockIdx.x;
+    // with row flags, a row whose mask row is empty only needs the next smoothing
+    const bool detail = !(MASK && row_flags && !row_flags[r]);
     const int nx4 = nx >> 2;
     const int nt = blockDim.x;
     const float4 *in4 = reinterpret_cast<const float4 *>(in);
@@ -169,11 +174,15 @@ atrous_pair(const float *__restrict__ in, const float *c0, const float *__restri
                  rp2 = (size_t)mirror(r + 2 * d, ny) * nx4, rm4 = (size_t)mirror(r - 4 * d, ny) * nx4,
                  rp4 = (size_t)mirror(r + 4 * d, ny) * nx4;
     for (int c4 = threadIdx.x; c4 < nx4; c4 += nt) {
-        const float4 c = __ldg(in4 + rc + c4), a = __ldg(in4 + rm2 + c4), b = __ldg(in4 + rm1 + c4),
-                     e = __ldg(in4 + rp1 + c4), f = __ldg(in4 + rp2 + c4), a2 = __ldg(in4 + rm4 + c4),
-                     f2 = __ldg(in4 + rp4 + c4);
-        smem4[c4] = b3_tap4(c, a, b, e, f);            // dilation d
+        const float4 c = __ldg(in4 + rc + c4), a = __ldg(in4 + rm2 + c4), f = __ldg(in4 + rp2 + c4),
+                     a2 = __ldg(in4 + rm4 + c4), f2 = __ldg(in4 + rp4 + c4);
+        float4 b = make_float4(0.f, 0.f, 0.f, 0.f), e = b;
+        if (detail) {
+            b = __ldg(in4 + rm1 + c4);
+            e = __ldg(in4 + rp1 + c4);
+        }
         smem4[nx4 + c4] = b3_tap4(c, a2, a, f, f2);    // dilation 2d: taps r -+ 4d, r -+ 2d
+        if (detail) smem4[c4] = b3_tap4(c, a, b, e, f);   // dilation d
     }
     __syncthreads();
     const float *band1 = reinterpret_cast<const float *>(smem4);
@@ -183,6 +192,10 @@ atrous_pair(const float *__restrict__ in, const float *c0, const float *__restri
     float4 *next4 = reinterpret_cast<float4 *>(next);
     for (int c4 = threadIdx.x; c4 < nx4; c4 += nt) {
         const size_t g4 = rc + c4;
+        if (!detail) {
+            next4[g4] = horizontal4(band2, c4 * 4, nx, 2 * d);
+            continue;
+        }
         const float4 x = c04[g4];
         float4 v = horizontal4(band1, c4 * 4, nx, d);
         v.x = __fsub_rn(x.x, v.x);
@@ -224,7 +237,7 @@ int band_rows_for(int, int) { return 1; }
 
 template <int EPI>
 int launch_band(const float *in, float *out, const float *aux, int ny, int nx, int d, cudaStream_t st,
-                const float *mask = nullptr) {
+                const float *mask = nullptr, const unsigned char *row_flags = nullptr) {
     static std::once_flag once;
     std::call_once(once, [] {
         cudaFuncSetAttribute(atrous_band<EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxSmem);
@@ -234,7 +247,7 @@ int launch_band(const float *in, float *out, const float *aux, int ny, int nx, i
     const int grid = (ny + band - 1) / band;
     const int work4 = band * (nx >> 2);
     const int threads = work4 >= kThreads ? kThreads : ((work4 + 31) / 32) * 32;
-    atrous_band<EPI><<<grid, threads, smem, st>>>(in, out, aux, mask, ny, nx, d, band);
+    atrous_band<EPI><<<grid, threads, smem, st>>>(in, out, aux, mask, ny, nx, d, band, row_flags);
     return check_launch("atrous_band");
 }
 
@@ -243,14 +256,15 @@ bool pair_fits(int nx) { return (size_t)2 * nx * sizeof(float) <= (size_t)kMaxSm
 
 template <bool MASK>
 int launch_pair(const float *in, const float *c0, const float *mask, float *w, float *next, int ny, int nx, int d,
-                cudaStream_t st) {
+                cudaStream_t st, const unsigned char *row_flags = nullptr) {
     static std::once_flag once;
     std::call_once(once, [] {
         cudaFuncSetAttribute(atrous_pair<MASK>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxSmem);
     });
     const int nx4 = nx >> 2;
     const int threads = nx4 >= kThreads ? kThreads : ((nx4 + 31) / 32) * 32;
-    atrous_pair<MASK><<<ny, threads, 2 * (size_t)nx * sizeof(float), st>>>(in, c0, mask, w, next, ny, nx, d);
+    atrous_pair<MASK><<<ny, threads, 2 * (size_t)nx * sizeof(float), st>>>(in, c0, mask, w, next, ny, nx, d,
+                                                                            row_flags);
     return check_launch("atrous_pair");
 }
 
@@ -294,14 +308,15 @@ int iuwt_smooth_add(const float *in, const float *w, float *out, int ny, int nx,
     return launch_band<kAdd>(in, out, w, ny, nx, 1 << scale, st);
 }
 int iuwt_smooth_detail_mask(const float *in, const float *c0, const float *mask, float *w, int ny, int nx, int scale,
-                            cudaStream_t st) {
-    return launch_band<kDetailMask>(in, w, c0, ny, nx, 1 << scale, st, mask);
+                            cudaStream_t st, const unsigned char *row_flags = nullptr) {
+    return launch_band<kDetailMask>(in, w, c0, ny, nx, 1 << scale, st, mask, row_flags);
 }
 
 // Decomposition as the reference sequences it: per scale one smoothing and one
 // detail pass (used for a single detail plane or rows too long for atrous_pair).
 int iuwt_decompose_unfused(const float *d_in, float *d_detail, float *d_smoothed, int ny, int nx, int scale_count,
-                           int scale_adjust, float *p0, float *p1, cudaStream_t st, const float *d_mask) {
+                           int scale_adjust, float *p0, float *p1, cudaStream_t st, const float *d_mask,
+                           const unsigned char *d_row_flags) {
     const size_t plane = (size_t)ny * nx;
     float *bufs[2] = {p0, p1};
     const float *cur = d_in;
@@ -320,7 +335,8 @@ int iuwt_decompose_unfused(const float *d_in, float *d_detail, float *d_smoothed
         MSN_TRY(iuwt_smooth(cur, c, ny, nx, s, st));
         float *w = d_detail + (size_t)(s - scale_adjust) * plane;
         if (d_mask)
-            MSN_TRY(iuwt_smooth_detail_mask(c, cur, d_mask + (size_t)(s - scale_adjust) * plane, w, ny, nx, s, st));
+            MSN_TRY(iuwt_smooth_detail_mask(c, cur, d_mask + (size_t)(s - scale_adjust) * plane, w, ny, nx, s, st,
+                                            d_row_flags ? d_row_flags + (size_t)(s - scale_adjust) * ny : nullptr));
         else
             MSN_TRY(iuwt_smooth_detail(c, cur, w, ny, nx, s, st));
         cur = c;
@@ -336,11 +352,17 @@ int iuwt_decompose_unfused(const float *d_in, float *d_detail, float *d_smoothed
 // Decomposition with the detail pass of scale s fused with the smoothing of
 // scale s + 1 (atrous_pair): scale_count - scale_adjust + 1 launches after the
 // warm-up smoothings instead of twice that. Scratch: the two planes p0, p1.
+// d_row_flags (masked only, may be null): [planes][ny] bytes, 0 where the mask
+// row is empty; such detail rows are not written (the caller keeps them zero).
 int iuwt_decompose_impl(const float *d_in, float *d_detail, float *d_smoothed, int ny, int nx, int scale_count,
-                        int scale_adjust, float *p0, float *p1, cudaStream_t st, const float *d_mask = nullptr) {
+                        int scale_adjust, float *p0, float *p1, cudaStream_t st, const float *d_mask = nullptr,
+                        const unsigned char *d_row_flags = nullptr) {
     if (scale_count - scale_adjust < 2 || !pair_fits(nx))
         return iuwt_decompose_unfused(d_in, d_detail, d_smoothed, ny, nx, scale_count, scale_adjust, p0, p1, st,
-                                      d_mask);
+                                      d_mask, d_row_flags);
+    auto flags_of = [&](int s) {
+        return d_row_flags ? d_row_flags + (size_t)(s - scale_adjust) * ny : nullptr;
+    };
     const size_t plane = (size_t)ny * nx;
     float *bufs[2] = {p0, p1};
     const float *cur = d_in;  // C_{s-1}: the detail epilogue's minuend
@@ -360,7 +382,7 @@ int iuwt_decompose_impl(const float *d_in, float *d_detail, float *d_smoothed, i
         float *next = (s == scale_count - 2 && d_smoothed) ? d_smoothed : bufs[1 - c_buf];
         if (d_mask)
             MSN_TRY(launch_pair<true>(c, cur, d_mask + (size_t)(s - scale_adjust) * plane, w, next, ny, nx, 1 << s,
-                                      st));
+                                      st, flags_of(s)));
         else
             MSN_TRY(launch_pair<false>(c, cur, nullptr, w, next, ny, nx, 1 << s, st));
         cur = c;
@@ -370,7 +392,8 @@ int iuwt_decompose_impl(const float *d_in, float *d_detail, float *d_smoothed, i
     const int s = scale_count - 1;
     float *w = d_detail + (size_t)(s - scale_adjust) * plane;
     if (d_mask)
-        MSN_TRY(iuwt_smooth_detail_mask(c, cur, d_mask + (size_t)(s - scale_adjust) * plane, w, ny, nx, s, st));
+        MSN_TRY(iuwt_smooth_detail_mask(c, cur, d_mask + (size_t)(s - scale_adjust) * plane, w, ny, nx, s, st,
+                                        flags_of(s)));
     else
         MSN_TRY(iuwt_smooth_detail(c, cur, w, ny, nx, s, st));
     return MSN_OK;
@@ -476,6 +499,25 @@ extern "C" int msn_iuwt_decompose_masked(const float *d_in, const float *d_mask,
     MSN_TRY(split_workspace(d_work, work_bytes, ny, nx, &p0, &p1, fn));
     return iuwt_decompose_impl(d_in, d_detail, nullptr, ny, nx, scale_count, scale_adjust, p0, p1, as_stream(stream),
                                d_mask);
+}
+
+extern "C" int msn_iuwt_decompose_masked_rows(const float *d_in, const float *d_mask, const unsigned char *d_row_flags,
+                                              float *d_detail, int ny, int nx, int scale_count, int scale_adjust,
+                                              void *d_work, size_t work_bytes, void *stream) {
+    clear_error();
+    static const char *fn = "msn_iuwt_decompose_masked_rows";
+    MSN_TRY(validate_image(ny, nx, fn));
+    MSN_TRY(validate_scales(ny, nx, scale_count, fn));
+    if (scale_adjust < 0 || scale_adjust > scale_count)
+        return set_error(MSN_ERR_INVALID, "%s: scale_adjust=%d outside [0, %d]", fn, scale_adjust, scale_count);
+    if (!d_in || !d_mask || !d_row_flags || (scale_count > scale_adjust && !d_detail))
+        return set_error(MSN_ERR_INVALID, "%s: null input, mask, row flags or detail pointer", fn);
+    if (!aligned16(d_in) || !aligned16(d_detail) || !aligned16(d_mask))
+        return set_error(MSN_ERR_INVALID, "%s: device pointers must be 16-byte aligned", fn);
+    float *p0, *p1;
+    MSN_TRY(split_workspace(d_work, work_bytes, ny, nx, &p0, &p1, fn));
+    return iuwt_decompose_impl(d_in, d_detail, nullptr, ny, nx, scale_count, scale_adjust, p0, p1, as_stream(stream),
+                               d_mask, d_row_flags);
 }
 
 extern "C" int msn_iuwt_recompose(const float *d_detail, int planes, const float *d_smoothed, float *d_out, int ny,

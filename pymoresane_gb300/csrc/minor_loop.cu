@@ -177,6 +177,7 @@ msn_minor_args make_key(const msn_minor_args *a) {
     k.snr2 = a->snr2;
     k.neg = a->neg;
     k.seg_flags = a->seg_flags;
+    k.row_flags = a->row_flags;
     k.fft_work = a->fft_work;
     k.fft_work_bytes = a->fft_work_bytes;
     k.iuwt_work = a->iuwt_work;
@@ -191,8 +192,9 @@ msn_minor_args make_key(const msn_minor_args *a) {
 int apply_a(const msn_minor_args *a, const float *in, float *out, cudaStream_t st) {
     const int planes = a->max_scale - a->scale_adjust;
     MSN_TRY(msn_fft_convolve(in, a->n, a->m, a->spec, a->tmp, a->linear, a->fft_work, a->fft_work_bytes, st));
-    MSN_TRY(msn_iuwt_decompose_masked(a->tmp, a->emask, a->planes, a->n, a->n, a->max_scale, a->scale_adjust,
-                                      a->iuwt_work, a->iuwt_work_bytes, st));
+    // rows whose mask row is empty stay zero (cleared in the prologue)
+    MSN_TRY(msn_iuwt_decompose_masked_rows(a->tmp, a->emask, a->row_flags, a->planes, a->n, a->n, a->max_scale,
+                                           a->scale_adjust, a->iuwt_work, a->iuwt_work_bytes, st));
     return msn_iuwt_recompose(a->planes, planes, nullptr, out, a->n, a->n, a->scale_adjust, a->iuwt_work,
                               a->iuwt_work_bytes, st);
 }
@@ -252,8 +254,11 @@ int build_graph(Engine *e, const msn_minor_args *a, CacheEntry *ce) {
         MSN_TRY(check_cuda(cudaMemsetAsync(a->ms, 0, (size_t)planes * nvec * sizeof(float), st), "zero sources"));
         MSN_TRY(check_cuda(cudaMemcpyAsync(a->r, a->rec, nvec * sizeof(float), cudaMemcpyDeviceToDevice, st), "r"));
         MSN_TRY(check_cuda(cudaMemcpyAsync(a->p, a->rec, nvec * sizeof(float), cudaMemcpyDeviceToDevice, st), "p"));
-        // the extraction mask is fixed for the whole minor loop: flag its non-empty segments once
+        // the extraction mask is fixed for the whole minor loop: flag its non-empty segments and
+        // rows once, and clear Q, whose rows outside the mask are then never written again
         MSN_TRY(msn_segment_flags(a->emask, (size_t)planes * nvec, a->seg_flags, st));
+        MSN_TRY(msn_row_flags(a->emask, (size_t)planes * a->n, a->n, a->row_flags, st));
+        MSN_TRY(check_cuda(cudaMemsetAsync(a->planes, 0, (size_t)planes * nvec * sizeof(float), st), "zero Q"));
         minor_init<<<1, 1, 0, st>>>(state, a->minor_loop_miter);
         MSN_TRY(check_launch("minor_init"));
         return add_conditional(st, while_h, cudaGraphCondTypeWhile, &body);
@@ -313,7 +318,7 @@ int validate_args(const msn_minor_args *a) {
     if (a->minor_loop_miter < 0) return set_error(MSN_ERR_INVALID, "%s: negative minor_loop_miter", fn);
     const void *ptrs[] = {a->spec, a->rec, a->x,     a->xn,   a->r,    a->rn,  a->p,        a->ap,
                           a->tmp,  a->planes, a->emask, a->esrc, a->ms, a->scal, a->snr2, a->neg,
-                          a->seg_flags, a->fft_work, a->iuwt_work, a->red_work};
+                          a->seg_flags, a->row_flags, a->fft_work, a->iuwt_work, a->red_work};
     for (const void *p : ptrs)
         if (p == nullptr) return set_error(MSN_ERR_INVALID, "%s: null buffer in the argument block", fn);
     const void *vecs[] = {a->rec, a->x, a->xn, a->r, a->rn, a->p, a->ap, a->tmp, a->planes, a->emask, a->esrc, a->ms};
@@ -479,7 +484,7 @@ int validate_run(const msn_moresane_args *a) {
     const void *ptrs[] = {a->dirty, a->energies, a->spec_sub, a->spec_data, a->model, a->residual, a->dec, a->thr,
                           a->emask, a->esrc, a->planes, a->ms, a->x, a->xn, a->r, a->rn, a->p, a->ap, a->tmp,
                           a->rec, a->masked, a->sub, a->conv_full, a->sigma, a->pmax, a->scal, a->snr2, a->std4,
-                          a->neg, a->seg_flags, a->fmax, a->small, a->iuwt_work, a->fft_work, a->fft_work_full, a->tool_work,
+                          a->neg, a->seg_flags, a->row_flags, a->fmax, a->small, a->iuwt_work, a->fft_work, a->fft_work_full, a->tool_work,
                           a->red_work};
     for (const void *p : ptrs)
         if (!p) return set_error(MSN_ERR_INVALID, "%s: null buffer in the argument block", fn);
@@ -553,6 +558,7 @@ int run_moresane(Engine *e, const msn_moresane_args *a, msn_moresane_result *res
     m.snr2 = a->snr2;
     m.neg = a->neg;
     m.seg_flags = a->seg_flags;
+    m.row_flags = a->row_flags;
     m.fft_work = a->fft_work;
     m.fft_work_bytes = a->fft_work_bytes;
     m.iuwt_work = a->iuwt_work;

@@ -143,3 +143,28 @@ def test_masked_decomposition_equals_product(cuda, shape, scales, adj):
     got = dev.iuwt_decompose_masked(x, mask, scales, adj)
     want = w * mask
     assert torch.equal(got.view(torch.int32), want.view(torch.int32))
+
+
+@pytest.mark.parametrize("n,scales,adj,blobs", [(64, 4, 0, 3), (256, 6, 1, 10), (128, 5, 0, 0), (512, 7, 2, 30),
+                                                 (96, 2, 1, 4)])
+def test_decompose_masked_rows_matches_dense(cuda, n, scales, adj, blobs):
+    """Skipping the mask's empty rows leaves exactly the dense masked decomposition (zeros compare equal)."""
+    from pymoresane_gb300 import _native
+    rng = np.random.default_rng(n + scales + blobs)
+    planes = scales - adj
+    mask = np.zeros((planes, n, n), np.float32)
+    for _ in range(blobs):
+        p, y, x = rng.integers(0, planes), rng.integers(0, n - 8), rng.integers(0, n - 8)
+        mask[p, y:y + rng.integers(1, 8), x:x + rng.integers(1, 8)] = 1.0
+    x = torch.from_numpy(rng.standard_normal((n, n)).astype(np.float32)).cuda()
+    m = torch.from_numpy(mask).cuda()
+    dense = dev.iuwt_decompose_masked(x, m, scales, adj)
+    flags = torch.empty(planes * n, dtype=torch.uint8, device="cuda")
+    st = dev.stream_handle()
+    _native.call("msn_row_flags", m.data_ptr(), planes * n, n, flags.data_ptr(), st)
+    assert np.array_equal(flags.cpu().numpy().astype(bool), (mask != 0).any(axis=2).reshape(-1))
+    out = torch.zeros_like(dense)
+    work = dev.iuwt_workspace(n, n, x.device)
+    _native.call("msn_iuwt_decompose_masked_rows", x.data_ptr(), m.data_ptr(), flags.data_ptr(), out.data_ptr(), n, n,
+                 scales, adj, work.data_ptr(), work.numel(), st)
+    assert np.array_equal(out.cpu().numpy(), dense.cpu().numpy())
