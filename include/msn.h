@@ -211,7 +211,10 @@ int msn_label(const float *d_img, int ny, int nx, int *d_labels, int *d_count, v
  * Scalar block d_scal (float64): [0] r.r  [1] p.Ap  [2] alpha  [3] rn.rn  [4] beta
  * ------------------------------------------------------------------------- */
 
-/* Scratch bytes for every reduction below. */
+/* Scratch bytes for every reduction below. Zero the workspace once after
+ * allocating it: it holds the completion counter of the single-launch
+ * reductions, which every call leaves at zero again. One workspace per stream
+ * (calls that overlap on the GPU must not share it). */
 size_t msn_reduce_workspace_bytes(void);
 
 /* d_out2[0] = sum a*b, d_out2[1] = sum c*d (c, d may both be NULL) in float64

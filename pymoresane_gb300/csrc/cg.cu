@@ -32,6 +32,61 @@ __device__ __forceinline__ double block_sum(double v) {
     return v;  // valid in thread 0
 }
 
+// Two-stage deterministic reduction in one launch: every CTA writes its
+// partial pair, and the last CTA to finish (completion counter after the
+// partials, reset to zero by that CTA) sums the kRedGrid pairs in a fixed
+// order -- thread t adds pairs t, t + 256, t + 512, then warp-shuffle trees --
+// so the totals do not depend on which CTA finishes last.
+__device__ __forceinline__ bool finish_pairs(double s0, double s1, double *__restrict__ partials, double *out,
+                                             double *beta_scal) {
+    __shared__ bool last;
+    __shared__ double ws[2][kRedThreads / 32];
+    s0 = block_sum(s0);
+    s1 = block_sum(s1);
+    unsigned *counter = reinterpret_cast<unsigned *>(partials + 2 * kRedGrid);
+    if (threadIdx.x == 0) {
+        partials[2 * blockIdx.x] = s0;
+        partials[2 * blockIdx.x + 1] = s1;
+        __threadfence();
+        last = atomicAdd(counter, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!last) return false;
+    const int t = threadIdx.x;
+    double a = 0.0, b = 0.0;
+    for (int k = t; k < (int)gridDim.x; k += kRedThreads) {
+        a += __ldcg(partials + 2 * k);
+        b += __ldcg(partials + 2 * k + 1);
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+        a += __shfl_xor_sync(0xffffffffu, a, off);
+        b += __shfl_xor_sync(0xffffffffu, b, off);
+    }
+    if ((t & 31) == 0) {
+        ws[0][t >> 5] = a;
+        ws[1][t >> 5] = b;
+    }
+    __syncthreads();
+    if (t < 32) {
+        a = t < kRedThreads / 32 ? ws[0][t] : 0.0;
+        b = t < kRedThreads / 32 ? ws[1][t] : 0.0;
+        for (int off = 16; off > 0; off >>= 1) {
+            a += __shfl_xor_sync(0xffffffffu, a, off);
+            b += __shfl_xor_sync(0xffffffffu, b, off);
+        }
+        if (t == 0) {
+            out[0] = a;
+            if (beta_scal) {
+                beta_scal[4] = a / beta_scal[0];  // beta = rn.rn / r.r (main.py:407-409)
+            } else {
+                out[1] = b;
+            }
+            *counter = 0u;
+        }
+    }
+    return true;
+}
+
 // Float64 accumulation at a low float64 instruction count (the FP64 rate of
 // GB300 is a small fraction of its FP32 rate): every thread forms the products
 // of four consecutive elements with a float32 fused multiply-add chain, then
@@ -51,7 +106,7 @@ __device__ __forceinline__ float sqdiff4(const float4 &a, const float4 &b) {
 template <bool DIFF>
 __global__ void __launch_bounds__(kRedThreads)
 dual_partials(const float4 *__restrict__ a, const float4 *__restrict__ b, const float4 *__restrict__ c,
-              const float4 *__restrict__ d, size_t n4, double *__restrict__ partials) {
+              const float4 *__restrict__ d, size_t n4, double *__restrict__ partials, double *__restrict__ out) {
     double s0 = 0.0, s1 = 0.0;
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n4; i += (size_t)gridDim.x * blockDim.x) {
         const float4 va = __ldg(a + i);
@@ -62,12 +117,7 @@ dual_partials(const float4 *__restrict__ a, const float4 *__restrict__ b, const 
             s1 += (double)dot4(__ldg(c + i), __ldg(d + i));
         }
     }
-    s0 = block_sum(s0);
-    s1 = block_sum(s1);
-    if (threadIdx.x == 0) {
-        partials[2 * blockIdx.x] = s0;
-        partials[2 * blockIdx.x + 1] = s1;
-    }
+    finish_pairs(s0, s1, partials, out, nullptr);
 }
 
 // Sums the kRedGrid partial pairs in a fixed order into out[0], out[1]: one
@@ -116,7 +166,7 @@ finalize_pairs(const double *__restrict__ partials, double *__restrict__ out) {
 __global__ void __launch_bounds__(kRedThreads)
 snr_update(const float4 *__restrict__ e, float4 *__restrict__ ms, const float4 *__restrict__ q,
            const double *__restrict__ scal, size_t n4, double *__restrict__ partials,
-           const unsigned char *__restrict__ seg_flags) {
+           const unsigned char *__restrict__ seg_flags, double *__restrict__ out) {
     const float a = (float)scal[S_ALPHA];
     double s0 = 0.0, s1 = 0.0;
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n4; i += (size_t)gridDim.x * blockDim.x) {
@@ -131,12 +181,7 @@ snr_update(const float4 *__restrict__ e, float4 *__restrict__ ms, const float4 *
         s0 += (double)dot4(ev, ev);
         s1 += (double)sqdiff4(ev, mv);
     }
-    s0 = block_sum(s0);
-    s1 = block_sum(s1);
-    if (threadIdx.x == 0) {
-        partials[2 * blockIdx.x] = s0;
-        partials[2 * blockIdx.x + 1] = s1;
-    }
+    finish_pairs(s0, s1, partials, out, nullptr);
 }
 
 // The vector updates evaluate the reference's float32 expressions
@@ -180,7 +225,7 @@ __global__ void cg_positivity(const float *__restrict__ x, float *__restrict__ x
 
 // rn = r - alpha Ap with the per-CTA float64 partial of rn . rn (main.py:405-408).
 __global__ void __launch_bounds__(kRedThreads)
-cg_residual(const float4 *__restrict__ r, const float4 *__restrict__ ap, const double *__restrict__ scal,
+cg_residual(const float4 *__restrict__ r, const float4 *__restrict__ ap, double *__restrict__ scal,
             float4 *__restrict__ rn, size_t n4, double *__restrict__ partials) {
     const float a = (float)scal[S_ALPHA];
     double s = 0.0;
@@ -194,11 +239,8 @@ cg_residual(const float4 *__restrict__ r, const float4 *__restrict__ ap, const d
         rn[i] = v;
         s += (double)dot4(v, v);
     }
-    s = block_sum(s);
-    if (threadIdx.x == 0) {
-        partials[2 * blockIdx.x] = s;
-        partials[2 * blockIdx.x + 1] = 0.0;
-    }
+    // scal[S_RNRN] = rn.rn, scal[S_BETA] = rn.rn / r.r
+    finish_pairs(s, 0.0, partials, scal + S_RNRN, scal);
 }
 
 // flags[s] = 1 when any element of float4 segment s (32 float4) of m is non-zero.
@@ -233,11 +275,6 @@ __global__ void row_flags(const float4 *__restrict__ m, size_t rows, int cols4, 
         const unsigned any = __any_sync(0xffffffffu, nz);
         if (lane == 0) flags[r] = any ? 1 : 0;
     }
-}
-
-__global__ void cg_beta(double *__restrict__ scal) {
-    // beta = rn.rn / r.r (main.py:407-409); S_RNRN was written by finalize_pairs.
-    scal[S_BETA] = scal[S_RNRN] / scal[S_RR];
 }
 
 // p = rn + beta p (main.py:411).
@@ -323,7 +360,9 @@ int ew_grid(size_t n) {
     return g < 1 ? 1 : (int)g;
 }
 
-constexpr size_t kPartialBytes = 2 * kRedGrid * sizeof(double);
+// kRedGrid partial pairs and the completion counter of finish_pairs (zero
+// between calls: the workspace is zeroed once when it is allocated).
+constexpr size_t kPartialBytes = 2 * kRedGrid * sizeof(double) + 16;
 
 }  // namespace
 
@@ -333,12 +372,10 @@ int dual_reduce(const float *a, const float *b, const float *c, const float *d, 
         return set_error(MSN_ERR_INVALID, "reduction: length must be a multiple of 4 and pointers 16-byte aligned");
     const float4 *a4 = (const float4 *)a, *b4 = (const float4 *)b, *c4 = (const float4 *)c, *d4 = (const float4 *)d;
     if (diff)
-        dual_partials<true><<<kRedGrid, kRedThreads, 0, st>>>(a4, b4, c4, d4, n / 4, partials);
+        dual_partials<true><<<kRedGrid, kRedThreads, 0, st>>>(a4, b4, c4, d4, n / 4, partials, out);
     else
-        dual_partials<false><<<kRedGrid, kRedThreads, 0, st>>>(a4, b4, c4, d4, n / 4, partials);
-    MSN_TRY(check_launch("dual_partials"));
-    finalize_pairs<<<1, kFinalizeThreads, 0, st>>>(partials, out);
-    return check_launch("finalize_pairs");
+        dual_partials<false><<<kRedGrid, kRedThreads, 0, st>>>(a4, b4, c4, d4, n / 4, partials, out);
+    return check_launch("dual_partials");
 }
 
 }  // namespace msn
@@ -380,10 +417,8 @@ extern "C" int msn_snr_update(const float *d_e, float *d_ms, const float *d_q, c
     cudaStream_t st = as_stream(stream);
     double *partials = (double *)d_work;
     snr_update<<<kRedGrid, kRedThreads, 0, st>>>((const float4 *)d_e, (float4 *)d_ms, (const float4 *)d_q, d_scal, n / 4,
-                                                  partials, nullptr);
-    MSN_TRY(check_launch("snr_update"));
-    finalize_pairs<<<1, kFinalizeThreads, 0, st>>>(partials, d_out2);
-    return check_launch("finalize_pairs");
+                                                  partials, nullptr, d_out2);
+    return check_launch("snr_update");
 }
 
 extern "C" size_t msn_segment_flags_bytes(size_t n) { return (n / 4 + 31) / 32; }
@@ -424,10 +459,8 @@ extern "C" int msn_snr_update_masked(const float *d_e, float *d_ms, const float 
     cudaStream_t st = as_stream(stream);
     double *partials = (double *)d_work;
     snr_update<<<kRedGrid, kRedThreads, 0, st>>>((const float4 *)d_e, (float4 *)d_ms, (const float4 *)d_q, d_scal, n / 4,
-                                                  partials, d_flags);
-    MSN_TRY(check_launch("snr_update"));
-    finalize_pairs<<<1, kFinalizeThreads, 0, st>>>(partials, d_out2);
-    return check_launch("finalize_pairs");
+                                                  partials, d_flags, d_out2);
+    return check_launch("snr_update");
 }
 
 extern "C" int msn_cg_alpha_x(const float *d_x, const float *d_p, double *d_scal, float *d_xn, size_t n,
@@ -461,11 +494,7 @@ extern "C" int msn_cg_residual(const float *d_r, const float *d_ap, double *d_sc
     double *partials = (double *)d_work;
     cg_residual<<<kRedGrid, kRedThreads, 0, st>>>((const float4 *)d_r, (const float4 *)d_ap, d_scal, (float4 *)d_rn,
                                                   n / 4, partials);
-    MSN_TRY(check_launch("cg_residual"));
-    finalize_pairs<<<1, kFinalizeThreads, 0, st>>>(partials, d_scal + S_RNRN);   // writes S_RNRN and S_RNRN+1 (= S_BETA, overwritten next)
-    MSN_TRY(check_launch("finalize_pairs"));
-    cg_beta<<<1, 1, 0, st>>>(d_scal);
-    return check_launch("cg_beta");
+    return check_launch("cg_residual");
 }
 
 extern "C" int msn_cg_direction(const float *d_rn, float *d_p, const double *d_scal, size_t n, void *stream) {

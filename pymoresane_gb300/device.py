@@ -322,7 +322,8 @@ def label(img, work=None):
 # ---------------------------------------------------------------------------
 
 def reduce_workspace(device):
-    return torch.empty(_native.query("msn_reduce_workspace_bytes"), dtype=torch.uint8, device=device)
+    """Reduction scratch, zeroed once (its completion counter must start at zero)."""
+    return torch.zeros(_native.query("msn_reduce_workspace_bytes"), dtype=torch.uint8, device=device)
 
 
 def dot2(a, b, c=None, d=None, out=None, work=None):
