@@ -274,6 +274,9 @@ int msn_model_update(float *d_model, int pitch, const float *d_x, int n_sub, int
 /* out = a - b (float32; pymoresane/main.py:485). */
 int msn_sub(const float *d_a, const float *d_b, float *d_out, size_t n, void *stream);
 
+/* out = a + b (float32; the residual added to the restored model, pymoresane/main.py:614). */
+int msn_add(const float *d_a, const float *d_b, float *d_out, size_t n, void *stream);
+
 /* out = a * b (float32; mask products, pymoresane/main.py:383,402,416). */
 int msn_mul(const float *d_a, const float *d_b, float *d_out, size_t n, void *stream);
 

@@ -64,6 +64,7 @@ SIGNATURES = {
     "msn_cg_direction": (c_int, [c_void_p, c_void_p, c_void_p, c_size_t, c_void_p]),
     "msn_model_update": (c_int, [c_void_p, c_int, c_void_p, c_int, c_int, c_int, c_float, c_int, c_void_p]),
     "msn_sub": (c_int, [c_void_p, c_void_p, c_void_p, c_size_t, c_void_p]),
+    "msn_add": (c_int, [c_void_p, c_void_p, c_void_p, c_size_t, c_void_p]),
     "msn_mul": (c_int, [c_void_p, c_void_p, c_void_p, c_size_t, c_void_p]),
     "msn_region_std": (c_int, [c_void_p, c_int, c_int, c_int, c_int, c_int, c_void_p, c_void_p, c_size_t, c_void_p]),
     "msn_minor_engine_create": (c_int, [ctypes.POINTER(c_void_p)]),

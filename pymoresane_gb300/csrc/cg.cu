@@ -309,6 +309,11 @@ __global__ void sub_kernel(const float *__restrict__ a, const float *__restrict_
         out[i] = __fsub_rn(a[i], b[i]);
 }
 
+__global__ void add_kernel(const float *__restrict__ a, const float *__restrict__ b, float *__restrict__ out, size_t n) {
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        out[i] = __fadd_rn(a[i], b[i]);
+}
+
 __global__ void mul_kernel(const float *__restrict__ a, const float *__restrict__ b, float *__restrict__ out, size_t n) {
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
         out[i] = __fmul_rn(a[i], b[i]);
@@ -521,6 +526,13 @@ extern "C" int msn_sub(const float *d_a, const float *d_b, float *d_out, size_t 
     if (!d_a || !d_b || !d_out) return set_error(MSN_ERR_INVALID, "msn_sub: null pointer");
     sub_kernel<<<ew_grid(n), 256, 0, as_stream(stream)>>>(d_a, d_b, d_out, n);
     return check_launch("sub");
+}
+
+extern "C" int msn_add(const float *d_a, const float *d_b, float *d_out, size_t n, void *stream) {
+    clear_error();
+    if (!d_a || !d_b || !d_out) return set_error(MSN_ERR_INVALID, "msn_add: null pointer");
+    add_kernel<<<ew_grid(n), 256, 0, as_stream(stream)>>>(d_a, d_b, d_out, n);
+    return check_launch("add");
 }
 
 extern "C" int msn_mul(const float *d_a, const float *d_b, float *d_out, size_t n, void *stream) {

@@ -22,6 +22,7 @@ import numpy as np
 import torch
 
 from . import _native
+from .beam_fit import beam_fit
 from . import device as dev
 from . import fits
 
@@ -633,6 +634,40 @@ class DataImage(object):
         self.model = model_acc.cpu().numpy()
         self.residual = residual.cpu().numpy()
         self.complete = False
+
+    def restore(self):
+        """Restored image: model convolved with the fitted clean beam, plus the residual (main.py:601-616).
+
+        The beam fit runs on the host (pymoresane_gb300.beam_fit); the
+        convolution (linear for a double-size PSF, circular for a same-size one,
+        as the reference) and the addition run on the GPU. Sets self.restored
+        (float32) and returns [bmaj, bmin, bpa].
+        """
+        clean_beam, beam_params = beam_fit(self.psf_data, self.cdelt1, self.cdelt2)
+        self.restore_with(clean_beam)
+        return beam_params
+
+    def restore_with(self, clean_beam):
+        """The GPU half of restore(): self.restored = model (*) clean_beam + residual (main.py:607-615)."""
+        n, p = tuple(self.dirty_data_shape), tuple(self.psf_data_shape)
+        if p == tuple(2 * d for d in n):
+            linear = True
+        elif p == n:
+            linear = False
+        else:
+            raise ValueError(f"restore needs a PSF of the image's size or twice it; got {p} for {n}")
+        dev.require_cuda()
+        device = torch.device("cuda", torch.cuda.current_device())
+        spec = dev.psf_spectrum(torch.from_numpy(np.ascontiguousarray(clean_beam, dtype=np.float32)).to(device),
+                                m=p[0], off_r=0, off_c=0)
+        model = torch.from_numpy(np.ascontiguousarray(self.model, dtype=np.float32)).to(device)
+        residual = torch.from_numpy(np.ascontiguousarray(self.residual, dtype=np.float32)).to(device)
+        beam_model = dev.fft_convolve(model, spec, linear)
+        restored = torch.empty_like(beam_model)
+        _native.call("msn_add", beam_model.data_ptr(), residual.data_ptr(), restored.data_ptr(), restored.numel(),
+                     dev.stream_handle())
+        self.restored = restored.cpu().numpy()
+        return self.restored
 
     # ------------------------------------------------------------------ outputs
     def save_fits(self, data, name):

@@ -26,3 +26,19 @@ def problem(n, psf_factor, seed):
     w = synthetic.Workload(n=n, psf_factor=psf_factor, n_uv=int(3000 * (n / 512) ** 2 * psf_factor ** 2 / 4) + 200,
                            n_points=10, n_gauss=2, sigma_range=(2.0, 5.0), noise=1e-3, seed=seed)
     return synthetic.make_problem(w)
+
+
+def restore_inputs():
+    """Seeded PSFs (3 sizes) and model / residual pairs of the restore fixtures (shared with the tests)."""
+    from pymoresane_gb300.synthetic import make_psf
+    psfs = {tag: make_psf(m, n_uv, np.random.default_rng(m)).astype(np.float32)
+            for tag, m, n_uv in (("p256", 256, 400), ("p512", 512, 900), ("p1024", 1024, 2500))}
+    rng = np.random.default_rng(7)
+    cases = {}
+    for tag, n, ptag in (("same", 256, "p256"), ("double", 256, "p512"), ("double512", 512, "p1024")):
+        model = np.zeros((n, n), np.float32)
+        idx = rng.integers(8, n - 8, (30, 2))
+        model[idx[:, 0], idx[:, 1]] = rng.uniform(0.1, 2.0, 30).astype(np.float32)
+        residual = (0.01 * rng.standard_normal((n, n))).astype(np.float32)
+        cases[tag] = (ptag, model, residual)
+    return psfs, cases

@@ -21,7 +21,7 @@ sys.path.insert(0, HERE)
 sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
 
 import refshim  # noqa: E402
-from cases import MORESANE_CASES, RUN_DEFAULTS, problem  # noqa: E402
+from cases import MORESANE_CASES, RUN_DEFAULTS, problem, restore_inputs  # noqa: E402
 
 
 def save(name, **arrays):
@@ -124,7 +124,31 @@ def gen_tart(ref):
     save("tart", model=img.model, residual=img.residual)
 
 
-GENERATORS = {"iuwt": gen_iuwt, "conv": gen_conv, "toolbox": gen_toolbox, "moresane": gen_moresane,
+def gen_restore(ref):
+    """beam_fit (beam_fit.py:6-69) on three PSF sizes and DataImage.restore (main.py:601-616).
+
+    The clean beams are stored as their non-zero bounding box (they are zero
+    elsewhere); the PSFs, models and residuals are regenerated from seeds.
+    """
+    psfs, cases = restore_inputs()
+    out = {}
+    for tag, psf in psfs.items():
+        beam, params = ref.beam_fit.beam_fit(psf, 0.5, 0.25)
+        nz = np.nonzero(beam)
+        r0, r1, c0, c1 = nz[0].min(), nz[0].max() + 1, nz[1].min(), nz[1].max() + 1
+        out[f"{tag}_beam_box"] = np.array([r0, r1, c0, c1])
+        out[f"{tag}_beam_crop"] = beam[r0:r1, c0:c1]
+        out[f"{tag}_params"] = np.asarray(params, np.float64)
+    for tag, (ptag, model, residual) in cases.items():
+        img = ref.main.DataImage(np.zeros_like(model), psfs[ptag], None, 0.5, 0.25)
+        img.model = model
+        img.residual = residual
+        out[f"{tag}_restore_params"] = np.asarray(img.restore(), np.float64)
+        out[f"{tag}_restored"] = img.restored
+    save("restore", **out)
+
+
+GENERATORS = {"restore": gen_restore, "iuwt": gen_iuwt, "conv": gen_conv, "toolbox": gen_toolbox, "moresane": gen_moresane,
               "tart": gen_tart}
 
 

@@ -15,6 +15,10 @@ Patches (all syntactic, none changes the arithmetic):
   main.py slice bounds (``/2``, ``/4``), iuwt_toolbox.py:29
   (``mid = in1.shape[1]/2``), iuwt_convolution.py:156 (``/4`` in pad_array)
   and iuwt_convolution.py:68 (``slice(0.5*sz, 1.5*sz)`` -> ints).
+* beam_fit.py:16 ``if psf.shape>512:`` compares a tuple with an int, which
+  Python 2 evaluates as True for every shape (a tuple sorts after an int) and
+  Python 3 rejects; it becomes ``if True:``, and the window bounds
+  ``psf.shape[i]/2-256`` use ``//`` (beam_fit.py:17), as Python 2 computed them.
 * The pycuda / scikits.cuda imports fail into the reference's own
   ``except`` blocks, so only the 'ser' / 'mp' / 'cpu' paths are usable.
 """
@@ -34,6 +38,9 @@ def _patch(name, src):
         src = re.sub(r"/(2|4)\b", r"//\1", src)
     if name == "iuwt_toolbox":
         src = src.replace("mid = in1.shape[1]/2", "mid = in1.shape[1]//2")
+    if name == "beam_fit":
+        src = src.replace("if psf.shape>512:", "if True:")
+        src = re.sub(r"psf\.shape\[(\d)\]/2", r"psf.shape[\1]//2", src)
     if name == "iuwt_convolution":
         src = src.replace("slice(0.5*sz,1.5*sz)", "slice(int(0.5*sz),int(1.5*sz))")
         src = src.replace("padded_size[0]/4:3*padded_size[0]/4,padded_size[1]/4:3*padded_size[1]/4",
