@@ -259,12 +259,29 @@ __device__ __forceinline__ int uf_find(const int *P, int x) {
     return x;
 }
 
+// Find with path halving: every visited node is re-pointed at its grandparent.
+// Parents always have smaller indices than their children (links are made with
+// atomicMin towards the smaller root), so the grandparent is an ancestor and
+// the store only shortens the path; a store that races a concurrent hook of
+// the same node at worst undoes a link that the hooking thread's retry (it
+// saw a non-root) makes again.
+__device__ __forceinline__ int uf_find_halve(int *P, int x) {
+    while (true) {
+        const int p = __ldcg(P + x);
+        if (p == x) return x;
+        const int gp = __ldcg(P + p);
+        if (gp == p) return p;
+        __stcg(P + x, gp);
+        x = gp;
+    }
+}
+
 __device__ __forceinline__ void uf_union(int *P, int a, int b) {
     // Lock-free: every failed hook means another thread lowered P[a]; indices
     // only decrease, so the loop terminates.
     while (true) {
-        a = uf_find(P, a);
-        b = uf_find(P, b);
+        a = uf_find_halve(P, a);
+        b = uf_find_halve(P, b);
         if (a == b) return;
         if (a < b) {
             const int t = a;
