@@ -67,14 +67,19 @@ mad_hist(const float *__restrict__ w, int ny, int nx, Rects rects, const SelectS
     const unsigned dmask = (unsigned)nbins - 1u;
     const float4 *w4 = reinterpret_cast<const float4 *>(w + (size_t)plane * ny * nx);
     const int nx4 = nx >> 2;
-    const size_t total4 = (size_t)ny * nx4;
-    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < total4; i += (size_t)gridDim.x * blockDim.x) {
+    const int total4 = ny * nx4;
+    const bool all_in = rects.y0 <= 0 && rects.y1 >= ny && rects.x0 <= 0 && rects.x1 >= nx && rects.ey0 >= rects.ey1;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total4; i += gridDim.x * blockDim.x) {
         const float4 v = __ldg(w4 + i);
-        const int y = (int)(i / nx4), x = (int)(i - (size_t)y * nx4) * 4;
+        int y = 0, x = 0;
+        if (!all_in) {
+            y = i / nx4;
+            x = (i - y * nx4) * 4;
+        }
         const float vals[4] = {v.x, v.y, v.z, v.w};
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
-            if (!in_rects(rects, y, x + k)) continue;
+            if (!all_in && !in_rects(rects, y, x + k)) continue;
             const unsigned key = __float_as_uint(vals[k]) & 0x7FFFFFFFu;
             const unsigned pre = hi >= 32 ? 0u : (key >> hi);
             const unsigned dig = (key >> shift) & dmask;
@@ -190,16 +195,24 @@ threshold_kernel(const float *__restrict__ w, int ny, int nx, const double *__re
     const float4 *w4 = reinterpret_cast<const float4 *>(w + base);
     float4 *o4 = reinterpret_cast<float4 *>(out + base);
     const int nx4 = nx >> 2;
-    const size_t total4 = (size_t)ny * nx4;
+    const int total4 = ny * nx4;
+    // For a float a, (double)a > thr exactly when a > thr rounded down to float
+    // (NaN and infinities included), so the reference's float64 comparison
+    // (iuwt_toolbox.py:70) needs no float64 arithmetic per element.
+    const float thr_f = __double2float_rd(thr);
     float mx = -FLT_MAX;
     bool any = false;
-    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < total4; i += (size_t)gridDim.x * blockDim.x) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total4; i += gridDim.x * blockDim.x) {
         const float4 v = __ldg(w4 + i);
-        const int y = (int)(i / nx4), x = (int)(i - (size_t)y * nx4) * 4;
         float vals[4] = {v.x, v.y, v.z, v.w};
+        int y = 0, x = 0;
+        if (supp) {
+            y = i / nx4;
+            x = (i - y * nx4) * 4;
+        }
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
-            const float keep = ((double)fabsf(vals[k]) > thr) ? 1.0f : 0.0f;
+            const float keep = (fabsf(vals[k]) > thr_f) ? 1.0f : 0.0f;
             float o = __fmul_rn(keep, vals[k]);
             if (supp) {
                 const bool inside = (y >= r0) & (y < r1) & (x + k >= c0) & (x + k < c1);
