@@ -91,6 +91,21 @@ int msn_iuwt_recompose(const float *d_detail, int planes, const float *d_smoothe
                        int ny, int nx, int scale_adjust, void *d_work, size_t work_bytes,
                        void *stream);
 
+/* Row activity of a recomposition started from zero whose detail stack is zero
+ * outside the rows flagged in d_row_flags [planes][ny] (msn_row_flags of the
+ * extraction mask): d_act [planes + scale_adjust][ny] bytes, level s active
+ * where any of its vertical taps at dilation 2^s in level s + 1 is active or
+ * its own detail row is flagged. No counterpart in the reference (support of
+ * msn_iuwt_recompose_rows for the minor loop's sparse A p). */
+int msn_recompose_row_activity(const unsigned char *d_row_flags, int planes, int ny, int scale_adjust,
+                               unsigned char *d_act, void *stream);
+
+/* msn_iuwt_recompose (no smoothed plane) computing only the rows d_act marks
+ * active and writing zeros elsewhere; equal to msn_iuwt_recompose on a detail
+ * stack that is zero outside the flagged rows (up to the sign of zeros). */
+int msn_iuwt_recompose_rows(const float *d_detail, int planes, const unsigned char *d_act, float *d_out, int ny,
+                            int nx, int scale_adjust, void *d_work, size_t work_bytes, void *stream);
+
 /* Same result as msn_iuwt_decompose, but the two scratch planes come from a
  * fixed device array inside libmsn.so instead of a caller workspace, so the
  * call allocates nothing. No counterpart in the reference: it exists for
@@ -324,6 +339,7 @@ typedef struct msn_minor_args {
     int *neg;               /* 1 int: #(xn < 0) */
     unsigned char *seg_flags; /* msn_segment_flags_bytes(planes * n * n) */
     unsigned char *row_flags; /* planes * n bytes */
+    unsigned char *rec_rows;  /* max_scale * n bytes: recomposition row activity */
     void *fft_work;         /* msn_fft_workspace_bytes(n, m) */
     size_t fft_work_bytes;
     void *iuwt_work;        /* msn_iuwt_workspace_bytes(n, n) */
@@ -418,6 +434,7 @@ typedef struct msn_moresane_args {
     int *neg;                /* 1 */
     unsigned char *seg_flags; /* msn_segment_flags_bytes(scale_count * ns * ns) */
     unsigned char *row_flags; /* scale_count * ns bytes */
+    unsigned char *rec_rows;  /* scale_count * ns bytes */
     float *fmax;             /* 1 */
     void *small;             /* >= 16 and >= 4 * scale_count bytes */
     size_t small_bytes;

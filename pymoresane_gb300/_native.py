@@ -26,6 +26,9 @@ SIGNATURES = {
                                           c_size_t, c_void_p]),
     "msn_iuwt_decompose_masked_rows": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_int, c_int, c_int,
                                                c_void_p, c_size_t, c_void_p]),
+    "msn_recompose_row_activity": (c_int, [c_void_p, c_int, c_int, c_int, c_void_p, c_void_p]),
+    "msn_iuwt_recompose_rows": (c_int, [c_void_p, c_int, c_void_p, c_void_p, c_int, c_int, c_int, c_void_p, c_size_t,
+                                        c_void_p]),
     "msn_iuwt_recompose": (c_int, [c_void_p, c_int, c_void_p, c_void_p, c_int, c_int, c_int, c_void_p, c_size_t,
                                    c_void_p]),
     "msn_iuwt_decompose_static": (c_int, [c_void_p, c_void_p, c_void_p, c_int, c_int, c_int, c_int, c_void_p]),
@@ -83,7 +86,8 @@ class MinorArgs(ctypes.Structure):
                 ("spec", c_void_p), ("rec", c_void_p), ("x", c_void_p), ("xn", c_void_p), ("r", c_void_p),
                 ("rn", c_void_p), ("p", c_void_p), ("ap", c_void_p), ("tmp", c_void_p), ("planes", c_void_p),
                 ("emask", c_void_p), ("esrc", c_void_p), ("ms", c_void_p), ("scal", c_void_p), ("snr2", c_void_p),
-                ("neg", c_void_p), ("seg_flags", c_void_p), ("row_flags", c_void_p), ("fft_work", c_void_p),
+                ("neg", c_void_p), ("seg_flags", c_void_p), ("row_flags", c_void_p), ("rec_rows", c_void_p),
+                ("fft_work", c_void_p),
                 ("fft_work_bytes", c_size_t),
                 ("iuwt_work", c_void_p),
                 ("iuwt_work_bytes", c_size_t), ("red_work", c_void_p), ("red_work_bytes", c_size_t)]
@@ -165,7 +169,7 @@ class MoresaneArgs(ctypes.Structure):
                                            "model", "residual", "dec", "thr", "emask", "esrc", "planes", "ms", "x",
                                            "xn", "r", "rn", "p", "ap", "tmp", "rec", "masked", "sub", "conv_full",
                                            "sigma", "pmax", "scal", "snr2", "std4", "neg", "seg_flags",
-                                           "row_flags", "fmax", "small")]
+                                           "row_flags", "rec_rows", "fmax", "small")]
                 + [("small_bytes", c_size_t)]
                 + [f for k in ("iuwt_work", "fft_work", "fft_work_full", "tool_work", "red_work")
                    for f in ((k, c_void_p), (k + "_bytes", c_size_t))])

@@ -91,6 +91,13 @@ atrous_band(const float *__restrict__ in, float *__restrict__ out, const float *
     extern __shared__ float4 smem4[];
     // masked detail with row flags: rows whose mask row is empty are left as they are (zero)
     if (EPI == kDetailMask && row_flags && band_rows == 1 && !row_flags[blockIdx.x]) return;
+    // recomposition with row activity: an inactive output row is exactly zero (all its
+    // taps and its detail row are zero), so it is written as zeros without reading anything
+    if ((EPI == kAdd || EPI == kStore) && row_flags && band_rows == 1 && !row_flags[blockIdx.x]) {
+        float4 *o4 = reinterpret_cast<float4 *>(out) + (size_t)blockIdx.x * (nx >> 2);
+        for (int j = threadIdx.x; j < (nx >> 2); j += blockDim.x) o4[j] = make_float4(0.f, 0.f, 0.f, 0.f);
+        return;
+    }
     const float *band = reinterpret_cast<const float *>(smem4);
     const int r0 = blockIdx.x * band_rows;
     const int rows = min(band_rows, ny - r0);
@@ -214,6 +221,29 @@ atrous_pair(const float *__restrict__ in, const float *c0, const float *__restri
     }
 }
 
+// Row activity of every level of a recomposition started from zero: the top
+// level (scale max_scale - 1) is active where its detail rows are (mask row
+// flags), each lower level where any of its five vertical taps at dilation 2^s
+// is active or its own detail row is; scales below scale_adjust have no detail.
+// One CTA, levels in sequence.
+__global__ void recompose_activity(const unsigned char *__restrict__ qrows, int planes, int ny, int scale_adjust,
+                                   unsigned char *__restrict__ act) {
+    const int top = planes + scale_adjust - 1;
+    for (int r = threadIdx.x; r < ny; r += blockDim.x) act[(size_t)top * ny + r] = qrows[(size_t)(planes - 1) * ny + r];
+    __syncthreads();
+    for (int s = top - 1; s >= 0; --s) {
+        const unsigned char *up = act + (size_t)(s + 1) * ny;
+        const int d = 1 << s;
+        for (int r = threadIdx.x; r < ny; r += blockDim.x) {
+            unsigned char a = up[r] | up[mirror(r - d, ny)] | up[mirror(r + d, ny)] | up[mirror(r - 2 * d, ny)] |
+                              up[mirror(r + 2 * d, ny)];
+            if (s >= scale_adjust) a |= qrows[(size_t)(s - scale_adjust) * ny + r];
+            act[(size_t)s * ny + r] = a ? 1 : 0;
+        }
+        __syncthreads();
+    }
+}
+
 // rec = 0 + w: the first recomposition step when no smoothed plane is given
 // (the smoothing of an all-zero plane is exactly +0, and +0 + w maps -0 to +0
 // exactly as the reference's addition does).
@@ -304,8 +334,9 @@ int iuwt_smooth(const float *in, float *out, int ny, int nx, int scale, cudaStre
 int iuwt_smooth_detail(const float *in, const float *c0, float *w, int ny, int nx, int scale, cudaStream_t st) {
     return launch_band<kDetail>(in, w, c0, ny, nx, 1 << scale, st);
 }
-int iuwt_smooth_add(const float *in, const float *w, float *out, int ny, int nx, int scale, cudaStream_t st) {
-    return launch_band<kAdd>(in, out, w, ny, nx, 1 << scale, st);
+int iuwt_smooth_add(const float *in, const float *w, float *out, int ny, int nx, int scale, cudaStream_t st,
+                    const unsigned char *row_act = nullptr) {
+    return launch_band<kAdd>(in, out, w, ny, nx, 1 << scale, st, nullptr, row_act);
 }
 int iuwt_smooth_detail_mask(const float *in, const float *c0, const float *mask, float *w, int ny, int nx, int scale,
                             cudaStream_t st, const unsigned char *row_flags = nullptr) {
@@ -399,8 +430,12 @@ int iuwt_decompose_impl(const float *d_in, float *d_detail, float *d_smoothed, i
     return MSN_OK;
 }
 
+// d_act (may be null): [max_scale][ny] bytes, row r of the level of scale s is
+// active when d_act[s * ny + r] != 0 (msn_recompose_row_activity); inactive rows
+// are written as zeros without being computed.
 int iuwt_recompose_impl(const float *d_detail, int planes, const float *d_smoothed, float *d_out, int ny, int nx,
-                        int scale_adjust, float *p0, float *p1, cudaStream_t st) {
+                        int scale_adjust, float *p0, float *p1, cudaStream_t st,
+                        const unsigned char *d_act = nullptr) {
     const size_t plane = (size_t)ny * nx;
     float *bufs[2] = {p0, p1};
     const int max_scale = planes + scale_adjust;
@@ -418,7 +453,7 @@ int iuwt_recompose_impl(const float *d_detail, int planes, const float *d_smooth
         if (cur == nullptr) {
             MSN_TRY(launch_zero_plus(w, dst, plane, st));
         } else {
-            MSN_TRY(iuwt_smooth_add(cur, w, dst, ny, nx, s, st));
+            MSN_TRY(iuwt_smooth_add(cur, w, dst, ny, nx, s, st, d_act ? d_act + (size_t)s * ny : nullptr));
         }
         cur = dst;
         cur_buf = (dst == d_out) ? -1 : nb;
@@ -428,6 +463,8 @@ int iuwt_recompose_impl(const float *d_detail, int planes, const float *d_smooth
         float *dst = dst_for(nb);
         if (cur == nullptr) {
             MSN_TRY(check_cuda(cudaMemsetAsync(dst, 0, plane * sizeof(float), st), "zero plane"));
+        } else if (d_act) {
+            MSN_TRY(launch_band<kStore>(cur, dst, nullptr, ny, nx, 1 << s, st, nullptr, d_act + (size_t)s * ny));
         } else {
             MSN_TRY(iuwt_smooth(cur, dst, ny, nx, s, st));
         }
@@ -518,6 +555,35 @@ extern "C" int msn_iuwt_decompose_masked_rows(const float *d_in, const float *d_
     MSN_TRY(split_workspace(d_work, work_bytes, ny, nx, &p0, &p1, fn));
     return iuwt_decompose_impl(d_in, d_detail, nullptr, ny, nx, scale_count, scale_adjust, p0, p1, as_stream(stream),
                                d_mask, d_row_flags);
+}
+
+extern "C" int msn_recompose_row_activity(const unsigned char *d_row_flags, int planes, int ny, int scale_adjust,
+                                          unsigned char *d_act, void *stream) {
+    clear_error();
+    if (!d_row_flags || !d_act || planes < 1 || ny < 1 || scale_adjust < 0)
+        return set_error(MSN_ERR_INVALID, "msn_recompose_row_activity: bad arguments");
+    if (2LL << (planes + scale_adjust - 1) > 2LL * ny)
+        return set_error(MSN_ERR_INVALID, "msn_recompose_row_activity: 2^%d exceeds the side %d",
+                         planes + scale_adjust, ny);
+    recompose_activity<<<1, 1024, 0, as_stream(stream)>>>(d_row_flags, planes, ny, scale_adjust, d_act);
+    return check_launch("recompose_activity");
+}
+
+extern "C" int msn_iuwt_recompose_rows(const float *d_detail, int planes, const unsigned char *d_act, float *d_out,
+                                       int ny, int nx, int scale_adjust, void *d_work, size_t work_bytes,
+                                       void *stream) {
+    clear_error();
+    static const char *fn = "msn_iuwt_recompose_rows";
+    MSN_TRY(validate_image(ny, nx, fn));
+    if (planes < 1 || scale_adjust < 0) return set_error(MSN_ERR_INVALID, "%s: bad plane count / adjust", fn);
+    MSN_TRY(validate_scales(ny, nx, planes + scale_adjust, fn));
+    if (!d_out || !d_detail || !d_act) return set_error(MSN_ERR_INVALID, "%s: null detail, activity or output", fn);
+    if (!aligned16(d_detail) || !aligned16(d_out))
+        return set_error(MSN_ERR_INVALID, "%s: device pointers must be 16-byte aligned", fn);
+    float *p0, *p1;
+    MSN_TRY(split_workspace(d_work, work_bytes, ny, nx, &p0, &p1, fn));
+    return iuwt_recompose_impl(d_detail, planes, nullptr, d_out, ny, nx, scale_adjust, p0, p1, as_stream(stream),
+                               d_act);
 }
 
 extern "C" int msn_iuwt_recompose(const float *d_detail, int planes, const float *d_smoothed, float *d_out, int ny,

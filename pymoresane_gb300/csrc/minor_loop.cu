@@ -178,6 +178,7 @@ msn_minor_args make_key(const msn_minor_args *a) {
     k.neg = a->neg;
     k.seg_flags = a->seg_flags;
     k.row_flags = a->row_flags;
+    k.rec_rows = a->rec_rows;
     k.fft_work = a->fft_work;
     k.fft_work_bytes = a->fft_work_bytes;
     k.iuwt_work = a->iuwt_work;
@@ -195,8 +196,9 @@ int apply_a(const msn_minor_args *a, const float *in, float *out, cudaStream_t s
     // rows whose mask row is empty stay zero (cleared in the prologue)
     MSN_TRY(msn_iuwt_decompose_masked_rows(a->tmp, a->emask, a->row_flags, a->planes, a->n, a->n, a->max_scale,
                                            a->scale_adjust, a->iuwt_work, a->iuwt_work_bytes, st));
-    return msn_iuwt_recompose(a->planes, planes, nullptr, out, a->n, a->n, a->scale_adjust, a->iuwt_work,
-                              a->iuwt_work_bytes, st);
+    // rows outside the recomposition's support (fixed for the minor loop) are written as zeros
+    return msn_iuwt_recompose_rows(a->planes, planes, a->rec_rows, out, a->n, a->n, a->scale_adjust, a->iuwt_work,
+                                   a->iuwt_work_bytes, st);
 }
 
 // Adds a conditional node after the current capture dependencies of st and
@@ -258,6 +260,7 @@ int build_graph(Engine *e, const msn_minor_args *a, CacheEntry *ce) {
         // rows once, and clear Q, whose rows outside the mask are then never written again
         MSN_TRY(msn_segment_flags(a->emask, (size_t)planes * nvec, a->seg_flags, st));
         MSN_TRY(msn_row_flags(a->emask, (size_t)planes * a->n, a->n, a->row_flags, st));
+        MSN_TRY(msn_recompose_row_activity(a->row_flags, planes, a->n, a->scale_adjust, a->rec_rows, st));
         MSN_TRY(check_cuda(cudaMemsetAsync(a->planes, 0, (size_t)planes * nvec * sizeof(float), st), "zero Q"));
         minor_init<<<1, 1, 0, st>>>(state, a->minor_loop_miter);
         MSN_TRY(check_launch("minor_init"));
@@ -318,7 +321,7 @@ int validate_args(const msn_minor_args *a) {
     if (a->minor_loop_miter < 0) return set_error(MSN_ERR_INVALID, "%s: negative minor_loop_miter", fn);
     const void *ptrs[] = {a->spec, a->rec, a->x,     a->xn,   a->r,    a->rn,  a->p,        a->ap,
                           a->tmp,  a->planes, a->emask, a->esrc, a->ms, a->scal, a->snr2, a->neg,
-                          a->seg_flags, a->row_flags, a->fft_work, a->iuwt_work, a->red_work};
+                          a->seg_flags, a->row_flags, a->rec_rows, a->fft_work, a->iuwt_work, a->red_work};
     for (const void *p : ptrs)
         if (p == nullptr) return set_error(MSN_ERR_INVALID, "%s: null buffer in the argument block", fn);
     const void *vecs[] = {a->rec, a->x, a->xn, a->r, a->rn, a->p, a->ap, a->tmp, a->planes, a->emask, a->esrc, a->ms};
@@ -484,7 +487,7 @@ int validate_run(const msn_moresane_args *a) {
     const void *ptrs[] = {a->dirty, a->energies, a->spec_sub, a->spec_data, a->model, a->residual, a->dec, a->thr,
                           a->emask, a->esrc, a->planes, a->ms, a->x, a->xn, a->r, a->rn, a->p, a->ap, a->tmp,
                           a->rec, a->masked, a->sub, a->conv_full, a->sigma, a->pmax, a->scal, a->snr2, a->std4,
-                          a->neg, a->seg_flags, a->row_flags, a->fmax, a->small, a->iuwt_work, a->fft_work, a->fft_work_full, a->tool_work,
+                          a->neg, a->seg_flags, a->row_flags, a->rec_rows, a->fmax, a->small, a->iuwt_work, a->fft_work, a->fft_work_full, a->tool_work,
                           a->red_work};
     for (const void *p : ptrs)
         if (!p) return set_error(MSN_ERR_INVALID, "%s: null buffer in the argument block", fn);
@@ -559,6 +562,7 @@ int run_moresane(Engine *e, const msn_moresane_args *a, msn_moresane_result *res
     m.neg = a->neg;
     m.seg_flags = a->seg_flags;
     m.row_flags = a->row_flags;
+    m.rec_rows = a->rec_rows;
     m.fft_work = a->fft_work;
     m.fft_work_bytes = a->fft_work_bytes;
     m.iuwt_work = a->iuwt_work;

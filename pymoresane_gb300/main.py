@@ -86,6 +86,7 @@ class _Buffers:
         self.seg_flags = torch.empty(max(1, _native.query("msn_segment_flags_bytes", s * ns * ns)), dtype=torch.uint8,
                                      device=device)
         self.row_flags = torch.empty(s * ns, dtype=torch.uint8, device=device)
+        self.rec_rows = torch.empty(s * ns, dtype=torch.uint8, device=device)
 
 
 _ENGINES = threading.local()
@@ -257,7 +258,7 @@ class Deconvolver:
         a.planes, a.emask, a.esrc, a.ms = (B.planes.data_ptr(), B.emask.data_ptr(), B.esrc.data_ptr(),
                                            B.ms.data_ptr())
         a.scal, a.snr2, a.neg = B.scal.data_ptr(), B.snr2.data_ptr(), B.neg.data_ptr()
-        a.seg_flags, a.row_flags = B.seg_flags.data_ptr(), B.row_flags.data_ptr()
+        a.seg_flags, a.row_flags, a.rec_rows = B.seg_flags.data_ptr(), B.row_flags.data_ptr(), B.rec_rows.data_ptr()
         a.fft_work, a.fft_work_bytes = B.fft_work.data_ptr(), B.fft_work.numel()
         a.iuwt_work, a.iuwt_work_bytes = B.iuwt_work.data_ptr(), B.iuwt_work.numel()
         a.red_work, a.red_work_bytes = B.red_work.data_ptr(), B.red_work.numel()
@@ -291,7 +292,7 @@ class Deconvolver:
         a.spec_data = spec_data.packed.data_ptr()
         a.model, a.residual = model.data_ptr(), residual.data_ptr()
         for k in ("dec", "thr", "emask", "esrc", "planes", "ms", "conv_full", "sigma", "pmax", "scal", "snr2",
-                  "std4", "neg", "seg_flags", "row_flags", "fmax", "small"):
+                  "std4", "neg", "seg_flags", "row_flags", "rec_rows", "fmax", "small"):
             setattr(a, k, getattr(B, k).data_ptr())
         for k in ("x", "xn", "r", "rn", "p", "ap", "tmp", "rec", "masked", "sub"):
             setattr(a, k, V[k].data_ptr())

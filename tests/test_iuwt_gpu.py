@@ -168,3 +168,33 @@ def test_decompose_masked_rows_matches_dense(cuda, n, scales, adj, blobs):
     _native.call("msn_iuwt_decompose_masked_rows", x.data_ptr(), m.data_ptr(), flags.data_ptr(), out.data_ptr(), n, n,
                  scales, adj, work.data_ptr(), work.numel(), st)
     assert np.array_equal(out.cpu().numpy(), dense.cpu().numpy())
+
+
+@pytest.mark.parametrize("n,planes,adj,blobs", [(64, 4, 0, 3), (256, 6, 1, 10), (128, 5, 0, 0), (512, 7, 2, 25),
+                                                 (96, 1, 1, 4)])
+def test_recompose_rows_matches_dense(cuda, n, planes, adj, blobs):
+    """Recomposition restricted to the active rows equals the dense one on a row-sparse stack (zeros compare equal)."""
+    from pymoresane_gb300 import _native
+    rng = np.random.default_rng(3 * n + planes + blobs)
+    w = np.zeros((planes, n, n), np.float32)
+    for _ in range(blobs):
+        p, y, x = rng.integers(0, planes), rng.integers(0, n - 8), rng.integers(0, n - 8)
+        h, wd = rng.integers(1, 8), rng.integers(1, 8)
+        w[p, y:y + h, x:x + wd] = rng.standard_normal((h, wd)).astype(np.float32)
+    wt = torch.from_numpy(w).cuda()
+    dense = dev.iuwt_recompose(wt, adj)
+    st = dev.stream_handle()
+    flags = torch.empty(planes * n, dtype=torch.uint8, device="cuda")
+    _native.call("msn_row_flags", wt.data_ptr(), planes * n, n, flags.data_ptr(), st)
+    act = torch.empty((planes + adj) * n, dtype=torch.uint8, device="cuda")
+    _native.call("msn_recompose_row_activity", flags.data_ptr(), planes, n, adj, act.data_ptr(), st)
+    out = torch.full((n, n), 7.0, device="cuda")          # stale contents must be overwritten
+    work = dev.iuwt_workspace(n, n, wt.device)
+    work.fill_(0x7f)
+    _native.call("msn_iuwt_recompose_rows", wt.data_ptr(), planes, act.data_ptr(), out.data_ptr(), n, n, adj,
+                 work.data_ptr(), work.numel(), st)
+    d = dense.cpu().numpy()
+    assert np.array_equal(out.cpu().numpy(), d)
+    # the activity covers every non-zero row of the result
+    rows = (d != 0).any(axis=1)
+    assert not np.any(rows & ~act.cpu().numpy()[:n].astype(bool))
