@@ -319,7 +319,8 @@ def run_deconv(args, rank, world, dist):
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
     total_ms, e2e_s = t.tolist()
     return {"ms": total_ms, "lat": lat, "e2e_s": e2e_s, "clocks": clocks, "traj": traj, "launches": n_launch,
-            "dirty": dirty_h, "psf": psf_h, "model_sum": float(img.model.sum()), "e2e_steps": e2e_steps}
+            "dirty": dirty_h, "psf": psf_h, "model_sum": float(img.model.sum()), "e2e_steps": e2e_steps,
+            "model": img.model.copy()}
 
 
 # ---------------------------------------------------------------------------
@@ -416,6 +417,23 @@ def run_serve(args, rank):
             "arrival_span_s": float(arrivals[-1]), "sizes": {int(n): int((sizes == n).sum()) for n in SERVE_SIZES}}
 
 
+def run_served_2048(args, dirty_h, psf_h, plain_model):
+    """The config-2 deconvolution served: args.served_jobs jobs submitted together to args.workers streams."""
+    from pymoresane_gb300.batch import DeconvolutionExecutor, Job
+    jobs = [Job(dirty_h, psf_h, kwargs=dict(DECONV_KW), tag=i) for i in range(args.served_jobs)]
+    with DeconvolutionExecutor(workers=args.workers, order="fifo") as ex:
+        ex.map(jobs[:args.workers])           # warm-up: every worker's buffers and graphs
+        t0 = time.perf_counter()
+        res = ex.map(jobs)
+        wall = time.perf_counter() - t0
+    lat = [r.latency * 1e3 for r in res]
+    return {"value": len(jobs) / wall, "unit": "deconv/s", "jobs": len(jobs), "workers": args.workers,
+            "latency_ms": {"p50": percentile(lat, 50), "p99": percentile(lat, 99),
+                           "mode": "all jobs submitted at once (queueing included)"},
+            "same_result_as_plain": bool(all(np.array_equal(r.model, plain_model) for r in res)),
+            "api": "pymoresane_gb300.batch.DeconvolutionExecutor.map with host numpy arrays"}
+
+
 def conv_roofline(n=2048, m=4096, reps=50):
     """Average duration of the fused linear convolution (the minor loop's dominant step) at 2048^2 / 4096^2.
 
@@ -465,6 +483,7 @@ def main():
     ap.add_argument("--requests", type=int, default=100, help="serve workload: requests")
     ap.add_argument("--rate", type=float, default=40.0, help="serve workload: arrivals per second")
     ap.add_argument("--distinct", type=int, default=3, help="batch / serve: distinct problems per size")
+    ap.add_argument("--served-jobs", type=int, default=8, help="deconv: jobs of the served 2048^2 measurement (0: skip)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--driver", default="native", choices=["native", "host"],
                     help="deconv: native = minor/major loops in libmsn (graphs); host = step by step (for ncu)")
@@ -599,6 +618,9 @@ def main():
         return
 
     res = run_deconv(args, rank, world, dist)
+    served = None
+    if args.served_jobs > 0 and args.driver == "native":
+        served = run_served_2048(args, res["dirty"], res["psf"], res["model"])
     ms_per_step = res["ms"] / args.steps
     value = world * args.steps / (res["ms"] * 1e-3)
     iuwt = measure_iuwt(5, 3, seed=rank)
@@ -632,6 +654,7 @@ def main():
                     "d2h_bytes_per_step": 8 * n * n, "steps": res["e2e_steps"],
                     "api": "pymoresane_gb300.main.DataImage(dirty, psf).moresane(...) with host numpy arrays"},
             "gpu_launches": res["launches"], "clocks": res["clocks"], "cpu_baseline": cpu,
+            "served": served,
         }))
     if dist:
         dist.destroy_process_group()

@@ -378,10 +378,14 @@ class Deconvolver:
             return img if ns == n else img[o:o + ns, o:o + ns].contiguous()
 
         def apply_a(vec_in, vec_out, max_scale, adj, planes):
+            # the same entry points as the native minor loop: the mask's empty rows are skipped in
+            # the decomposition (Q is cleared at the start of the minor loop) and the recomposition
+            # computes only the rows of its support (B.rec_rows)
             dev.fft_convolve(vec_in, spec_sub, linear, out=V["tmp"], work=B.fft_work)
-            w = B.planes[:planes]
-            dev.iuwt_decompose_masked(V["tmp"], B.emask, max_scale, adj, out=w, work=B.iuwt_work)
-            dev.iuwt_recompose(w, adj, out=vec_out, work=B.iuwt_work)
+            call("msn_iuwt_decompose_masked_rows", V["tmp"].data_ptr(), B.emask.data_ptr(), B.row_flags.data_ptr(),
+                 B.planes.data_ptr(), ns, ns, max_scale, adj, B.iuwt_work.data_ptr(), B.iuwt_work.numel(), st)
+            call("msn_iuwt_recompose_rows", B.planes.data_ptr(), planes, B.rec_rows.data_ptr(), vec_out.data_ptr(),
+                 ns, ns, adj, B.iuwt_work.data_ptr(), B.iuwt_work.numel(), st)
 
         def residual_of(model):
             res = torch.empty((n, n), dtype=torch.float32, device=dirty.device)
@@ -457,6 +461,12 @@ class Deconvolver:
                     x.zero_()
                     if self.incremental_snr:
                         B.ms[:planes].zero_()
+                    # supports of the (fixed) extraction mask, as the native minor loop's prologue
+                    B.planes[:planes].zero_()
+                    call("msn_segment_flags", B.emask.data_ptr(), planes * nvec, B.seg_flags.data_ptr(), st)
+                    call("msn_row_flags", B.emask.data_ptr(), planes * ns, ns, B.row_flags.data_ptr(), st)
+                    call("msn_recompose_row_activity", B.row_flags.data_ptr(), planes, ns, scale_adjust,
+                         B.rec_rows.data_ptr(), st)
                     r.copy_(V["rec"])
                     p.copy_(V["rec"])
                     minor = 0
@@ -477,9 +487,9 @@ class Deconvolver:
                         # model_sources = mask * W(H xn) and the SNR against the extracted sources
                         if self.incremental_snr:
                             # ms += alpha * (mask * W(H p)), the plane stack left in B.planes by apply_a
-                            call("msn_snr_update", B.esrc.data_ptr(), B.ms.data_ptr(), B.planes.data_ptr(),
-                                 B.scal.data_ptr(), planes * nvec, B.snr2.data_ptr(), B.red_work.data_ptr(),
-                                 B.red_work.numel(), st)
+                            call("msn_snr_update_masked", B.esrc.data_ptr(), B.ms.data_ptr(), B.planes.data_ptr(),
+                                 B.scal.data_ptr(), planes * nvec, B.seg_flags.data_ptr(), B.snr2.data_ptr(),
+                                 B.red_work.data_ptr(), B.red_work.numel(), st)
                         else:
                             dev.fft_convolve(xn, spec_sub, linear, out=V["tmp"], work=B.fft_work)
                             w = B.planes[:planes]
