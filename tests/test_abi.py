@@ -76,3 +76,27 @@ def test_minor_structs_match_header(tmp_path):
         cls = structs[cname]
         got = ctypes.sizeof(cls) if field == "size" else getattr(cls, field).offset
         assert got == int(value), (cname, field, got, value)
+
+
+def test_native_run_log_replay(caplog):
+    """The events of msn_moresane_run become the reference's log messages, in order (no GPU involved)."""
+    import logging
+
+    from pymoresane_gb300 import main as M
+    N = _native
+    evs = (N.Event * 9)()
+    spec = [(N.EV_MINIMUM_SCALE, 0, 0, 0.0), (N.EV_MAXIMUM_SCALE, 3, 0, 0.0), (N.EV_SCALE_EMPTY, 1, 0, 0.0),
+            (N.EV_MINOR_DONE, 7, N.MINOR_CONVERGED, 41.0), (N.EV_MINOR_DONE, 1, N.MINOR_FALSE_DETECTION, 45.0),
+            (N.EV_REVERTED, 0, 0, 0.0), (N.EV_MAJOR_DONE, 2, 0, 0.0), (N.EV_ALL_SCALES_POOR, 0, 0, 0.0),
+            (N.EV_NO_WORK, 0, 0, 0.0)]
+    for e, (c, a, b, v) in zip(evs, spec):
+        e.code, e.a, e.b, e.v = c, a, b, v
+    with caplog.at_level(logging.INFO, logger="pymoresane_gb300.main"):
+        M._replay(evs)
+    assert [r.getMessage() for r in caplog.records] == [
+        "Minimum scale = 0", "Maximum scale = 3", "Scale 1 is empty. Ignoring scales <= 1",
+        "Model has reached <1% error - exiting minor loop.", "7 minor loop iterations performed.",
+        "SNR too large on first iteration - false detection. Incrementing the minimum scale.",
+        "1 minor loop iterations performed.", "Residual has worsened - reverting changes.",
+        "2 major loop iterations performed.", "All scales are performing poorly - stopping.",
+        "Current MORESANE iteration did no work - finished."]
