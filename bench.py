@@ -32,6 +32,8 @@ import numpy as np
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
+from pymoresane_gb300 import replicas  # noqa: E402  (host-side rank coordination)
+sys.path.insert(0, ROOT)
 
 PEAKS_PATH = os.path.join(ROOT, "MEASURED_PEAKS.json")
 FALLBACK_HBM_GBS = 6800.0
@@ -314,10 +316,7 @@ def run_deconv(args, rank, world, dist):
         _ = float(img.model.sum())
     e2e_s = (time.perf_counter() - t0) / e2e_steps
 
-    t = torch.tensor([total_ms, e2e_s], dtype=torch.float64, device="cuda")
-    if dist:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    total_ms, e2e_s = t.tolist()
+    total_ms, e2e_s = replicas.reduce_max([total_ms, e2e_s], dist, "cuda")
     return {"ms": total_ms, "lat": lat, "e2e_s": e2e_s, "clocks": clocks, "traj": traj, "launches": n_launch,
             "dirty": dirty_h, "psf": psf_h, "model_sum": float(img.model.sum()), "e2e_steps": e2e_steps,
             "model": img.model.copy()}
@@ -362,14 +361,14 @@ def run_plain(jobs):
 def run_batch(args, rank):
     """64 images of sizes {256..2048} (p = .2 .3 .25 .15 .1), batched vs one at a time."""
     from pymoresane_gb300.batch import DeconvolutionExecutor
-    rng = np.random.default_rng(1000 + rank)
+    rng = np.random.default_rng(replicas.rank_seed(1000, rank))
     sizes = rng.choice(BATCH_SIZES, size=args.images, p=BATCH_P)
     cache = {}
     jobs = []
     for i, n in enumerate(sizes):
         key = (int(n), i % args.distinct)
         if key not in cache:
-            cache[key] = mix_job(int(n), seed=2000 + 97 * key[1] + int(n))
+            cache[key] = mix_job(int(n), seed=replicas.rank_seed(2000 + 97 * key[1] + int(n), rank))
         jobs.append(cache[key])
     # warm-up: one job per size through both paths (allocator pools, PSF plans, graph capture code)
     warm = [cache[k] for k in sorted({(k[0], 0) for k in cache})]
@@ -390,7 +389,7 @@ def run_batch(args, rank):
 def run_serve(args, rank):
     """Poisson arrivals (lambda = 40/s) of sizes {512..4096} (p = .35 .3 .15 .15 .05), served vs one at a time."""
     from pymoresane_gb300.batch import serve
-    rng = np.random.default_rng(3000 + rank)
+    rng = np.random.default_rng(replicas.rank_seed(3000, rank))
     sizes = rng.choice(SERVE_SIZES, size=args.requests, p=SERVE_P)
     arrivals = np.cumsum(rng.exponential(1.0 / args.rate, size=args.requests))
     cache = {}
@@ -398,7 +397,7 @@ def run_serve(args, rank):
     for i, n in enumerate(sizes):
         key = (int(n), i % args.distinct)
         if key not in cache:
-            cache[key] = mix_job(int(n), seed=4000 + 97 * key[1] + int(n))
+            cache[key] = mix_job(int(n), seed=replicas.rank_seed(4000 + 97 * key[1] + int(n), rank))
         jobs.append(cache[key])
     warm = [cache[k] for k in sorted({(k[0], 0) for k in cache})]
     run_plain(warm)
@@ -551,19 +550,23 @@ def main():
             sampler.start()
         r = run_batch(args, rank) if args.workload == "batch" else run_serve(args, rank)
         clocks = sampler.stop() if sampler else None
+        n_img = r["images"] if args.workload == "batch" else r["requests"]
+        mixed_s, plain_s = replicas.reduce_max([r["batch_s"] if args.workload == "batch" else r["wall_s"],
+                                                r["plain_s"]], dist, "cuda")
+        r["plain_s"] = plain_s
         if rank == 0:
-            n_img = r["images"] if args.workload == "batch" else r["requests"]
-            mixed_s = r["batch_s"] if args.workload == "batch" else r["wall_s"]
             line = {
                 "metric": ("64-image mixed-size batch, images/s (batched vs one at a time)" if args.workload == "batch"
                            else f"served deconvolutions/s under Poisson arrivals (lambda={args.rate:g}/s)"),
-                "value": world * n_img / mixed_s, "unit": "images/s", "n_gpus": world, "steps": 1, "warmup": 1,
+                "value": replicas.whole_job_rate(n_img, world, mixed_s), "unit": "images/s", "n_gpus": world,
+                "steps": 1, "warmup": 1,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
                 "data": "synthetic",
                 "config": {"workload": args.workload, "workers": args.workers, "sizes": r["sizes"],
                            "distinct_problems_per_size": args.distinct,
                            "parallelism": f"{args.workers} streams x {world} replicas"},
-                "plain": {"value": n_img / r["plain_s"], "unit": "images/s", "seconds": r["plain_s"]},
+                "plain": {"value": replicas.whole_job_rate(n_img, world, r["plain_s"]), "unit": "images/s",
+                          "seconds": r["plain_s"]},
                 "speedup_vs_plain": r["plain_s"] / mixed_s,
                 "latency_ms": {"p50": percentile(r["lat"], 50), "p99": percentile(r["lat"], 99)},
                 "clocks": clocks,
@@ -586,10 +589,7 @@ def main():
         if dist:
             dist.barrier()
         r = measure_iuwt(args.steps, args.warmup, seed=rank)
-        t = torch.tensor([r["ms_per_step"]], dtype=torch.float64, device="cuda")
-        if dist:
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+        ms = replicas.reduce_max([r["ms_per_step"]], dist, "cuda")[0]
         clocks = sampler.stop() if sampler else None
         e2e_s = iuwt_e2e(max(1, min(args.steps, 5)), seed=rank)
         n, s = IUWT_N, IUWT_S
