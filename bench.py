@@ -228,7 +228,7 @@ def cpu_iuwt(workers):
 
 def deconv_problem(seed):
     from pymoresane_gb300 import synthetic
-    dirty, psf, _ = synthetic.make_problem(synthetic.config2(seed))
+    dirty, psf, _ = synthetic.make_problem(synthetic.problem_2048(seed))
     return dirty, psf
 
 
@@ -333,7 +333,7 @@ MIX_KW = dict(sigma_level=4, loop_gain=0.2, tolerance=0.75, accuracy=1e-6, major
 
 
 def mix_job(n, seed):
-    """Config-0 style problem scaled by area to side n (PSF 2n, uv count and sources ~ n^2), S = log2(n) - 3."""
+    """The 512^2 problem's recipe scaled by area to side n (PSF 2n, uv count and sources ~ n^2), S = log2(n) - 3."""
     from pymoresane_gb300 import synthetic
     from pymoresane_gb300.batch import Job
     dirty, psf, _ = synthetic.make_problem(synthetic.scaled(n, seed=seed))
@@ -417,7 +417,7 @@ def run_serve(args, rank):
 
 
 def run_served_2048(args, dirty_h, psf_h, plain_model):
-    """The config-2 deconvolution served: args.served_jobs jobs submitted together to args.workers streams."""
+    """The 2048^2 deconvolution served: args.served_jobs jobs submitted together to args.workers streams."""
     from pymoresane_gb300.batch import DeconvolutionExecutor, Job
     jobs = [Job(dirty_h, psf_h, kwargs=dict(DECONV_KW), tag=i) for i in range(args.served_jobs)]
     with DeconvolutionExecutor(workers=args.workers, order="fifo") as ex:
@@ -436,7 +436,7 @@ def run_served_2048(args, dirty_h, psf_h, plain_model):
 def conv_roofline(n=2048, m=4096, reps=50):
     """Average duration of the fused linear convolution (the minor loop's dominant step) at 2048^2 / 4096^2.
 
-    Algorithmic bytes per convolution (SURVEY 8(d)): read x (4 n^2) + read the
+    Algorithmic bytes per convolution: read x (4 n^2) + read the
     PSF spectrum (8 m (m/2 + 1)) + write the result (4 n^2).
     """
     import torch
@@ -603,7 +603,7 @@ def main():
                 "metric": metric, "value": world * alg / (ms * 1e-3) / 1e9, "unit": unit, "n_gpus": world,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-                "config": {"workload": "iuwt_4096x4096_S8_store_smoothed (BASELINE config 1)",
+                "config": {"workload": "iuwt_4096x4096_S8_store_smoothed",
                            "l2": "working set 0.7 GB per step > 129 MB L2 (no flush needed)",
                            "parallelism": f"replicas x{world}"},
                 "roofline": {"bound": "hbm", "kernel": "atrous_band", "achieved": r["kernel_gbs"], "peak": hbm_peak,
@@ -637,7 +637,7 @@ def main():
             "metric": metric, "value": value, "unit": unit, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": "moresane_2048x2048_psf4096_S7_linear (BASELINE config 2)",
+            "config": {"workload": "moresane_2048x2048_psf4096_S7_linear",
                        "trajectory_major_minor": list(res["traj"]), "driver": args.driver,
                        "l2": "working set > 0.6 GB per deconvolution > 129 MB L2 (no flush needed)",
                        "parallelism": f"replicas x{world}"},

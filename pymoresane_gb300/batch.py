@@ -246,7 +246,7 @@ class DeconvolutionExecutor:
                     nonlocal held
                     freed = ws.drop_other_geometries(n, scale_count)
                     if freed:
-                        # cached blocks stay in this stream's pool unless handed back to the driver
+                        # cached blocks stay in this stream's pool unless handed back to CUDA
                         torch.cuda.empty_cache()
                     held -= freed
                     return freed

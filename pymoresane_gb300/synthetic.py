@@ -86,20 +86,20 @@ def make_problem(w: Workload):
     return dirty.astype(np.float32), psf, sky
 
 
-def config0(seed=0):
+def problem_512(seed=0):
     """512^2 dirty image, 1024^2 PSF, 3000 uv points, 40 points, 5 Gaussians."""
     return Workload(n=512, n_uv=3000, n_points=40, flux_range=(0.01, 1.0), n_gauss=5,
                     sigma_range=(2.0, 8.0), noise=1e-3, seed=seed)
 
 
-def config2(seed=0):
+def problem_2048(seed=0):
     """2048^2 dirty image, 4096^2 PSF, 20000 uv points, 1000 points, 50 Gaussians."""
     return Workload(n=2048, n_uv=20000, n_points=1000, flux_range=(1e-3, 1.0), n_gauss=50,
                     sigma_range=(2.0, 20.0), noise=1e-4, seed=seed)
 
 
 def scaled(n, seed=0):
-    """Config-0 style problem scaled by area to side n (uv count and sources)."""
+    """The 512^2 problem's recipe scaled by area to side n (uv count and sources)."""
     f = (n / 512.0) ** 2
     return Workload(n=n, n_uv=int(3000 * f), n_points=max(4, int(40 * f)), flux_range=(0.01, 1.0),
                     n_gauss=max(1, int(round(5 * f))), sigma_range=(2.0, 8.0), noise=1e-3, seed=seed)
