@@ -100,3 +100,14 @@ def test_native_run_log_replay(caplog):
         "1 minor loop iterations performed.", "Residual has worsened - reverting changes.",
         "2 major loop iterations performed.", "All scales are performing poorly - stopping.",
         "Current MORESANE iteration did no work - finished."]
+
+
+def test_engine_entry_points_reject_null_engine(lib):
+    """Argument checks that run before any CUDA call: a null engine is an invalid argument."""
+    args, res = _native.MinorArgs(), _native.MinorResult()
+    with pytest.raises(ValueError, match="null engine"):
+        _native.call("msn_minor_loop", None, ctypes.byref(args), ctypes.byref(res), None, 0, None)
+    margs, mres = _native.MoresaneArgs(), _native.MoresaneResult()
+    with pytest.raises(ValueError, match="null engine"):
+        _native.call("msn_moresane_run", None, ctypes.byref(margs), ctypes.byref(mres), None, 0, None, 0, None)
+    assert _native.query("msn_minor_engine_destroy", None) == 0

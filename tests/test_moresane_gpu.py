@@ -173,3 +173,29 @@ def test_native_major_loop_matches_host_major_loop(cuda, name, caplog):
     keys = ("major", "max_scale", "scale_adjust", "minor", "reverted")
     assert [[r[k] for k in keys] for r in la] == [[r[k] for k in keys] for r in lb]
     assert ga == gb
+
+
+def test_engine_rejects_bad_arguments(cuda):
+    """msn_minor_loop / msn_moresane_run validate their argument blocks before touching the device."""
+    import ctypes
+
+    from pymoresane_gb300 import _native
+    h = ctypes.c_void_p()
+    _native.call("msn_minor_engine_create", ctypes.byref(h))
+    try:
+        a, r = _native.MinorArgs(), _native.MinorResult()
+        a.n, a.max_scale, a.scale_adjust, a.minor_loop_miter = 30, 3, 0, 5      # n not a multiple of 4
+        with pytest.raises(ValueError, match="multiple of 4"):
+            _native.call("msn_minor_loop", h, ctypes.byref(a), ctypes.byref(r), None, 0, None)
+        a.n, a.max_scale = 64, 7                                                  # 2^7 > 64
+        with pytest.raises(ValueError, match="exceeds the side"):
+            _native.call("msn_minor_loop", h, ctypes.byref(a), ctypes.byref(r), None, 0, None)
+        a.max_scale = 3                                                           # buffers missing
+        with pytest.raises(ValueError, match="null buffer"):
+            _native.call("msn_minor_loop", h, ctypes.byref(a), ctypes.byref(r), None, 0, None)
+        m, mr = _native.MoresaneArgs(), _native.MoresaneResult()
+        m.n, m.ns, m.off, m.scale_count = 64, 32, 40, 3                           # subregion outside the image
+        with pytest.raises(ValueError, match="bad sides"):
+            _native.call("msn_moresane_run", h, ctypes.byref(m), ctypes.byref(mr), None, 0, None, 0, None)
+    finally:
+        _native.query("msn_minor_engine_destroy", h)
