@@ -50,3 +50,19 @@ def test_serve_reports_latency(cuda):
     assert all(r is not None for r in results)
     assert all(r.t_start >= r.t_submit and r.t_end > r.t_start for r in results)
     assert wall >= 0.5
+
+
+@pytest.mark.gpu
+def test_failing_job_reports_and_releases(cuda):
+    # an odd-sized image is rejected (main.py:101-103); the error reaches the caller's future,
+    # the job's memory reservation is returned and the other jobs still complete
+    from pymoresane_gb300.batch import DeconvolutionExecutor, Job
+    jobs = _jobs()[:2]
+    bad = Job(np.zeros((127, 127), np.float32), jobs[0].psf, kwargs=dict(KW, scale_count=3), tag="bad")
+    with DeconvolutionExecutor(workers=2) as ex:
+        futs = [ex.submit(j) for j in (jobs[0], bad, jobs[1])]
+        with pytest.raises(ValueError, match="uneven"):
+            futs[1].result(timeout=300)
+        assert futs[0].result(timeout=300).major >= 0 and futs[2].result(timeout=300).major >= 0
+    # every reservation (jobs' transients, workers' cached buffers) is returned at shutdown
+    assert ex.gate.used == 0
