@@ -49,9 +49,10 @@ def test_plans_for_every_supported_length(tmp_path):
     for m, ok, prod, twlen_ok, twbase_ok, e, fusable, direct, groups_ok in rows[:-1]:
         assert ok == 1 and prod == m and twlen_ok and twbase_ok and groups_ok, m
         assert e == (24 if m % 3 == 0 else 16)
-        if m >= 256:
-            # the fused PSF product and the global-fed / global-stored passes serve every grid a
-            # linear convolution of a 128^2 or larger image uses (smaller grids, and 192 = 3 * 64
-            # whose first radix-8 stride is not a multiple of 16, take the staged kernels)
-            assert fusable and direct, m
+        # global-fed / global-stored passes for every grid from 256 and 384 up; the PSF product
+        # fused between the column passes up to 6144 (8192's fused pass would need 1024 threads,
+        # and 192 = 3 * 64 has a first radix-8 stride that is not a multiple of 16): smaller grids
+        # and 8192 columns take the staged kernels
+        assert direct == (m >= 256 and m != 192), m
+        assert fusable == (m >= 256 and m != 192 and m != 8192), m
     assert rows[-1] == [0, 0]   # unsupported lengths are refused
