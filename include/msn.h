@@ -117,7 +117,10 @@ int msn_iuwt_recompose_rows(const float *d_detail, int planes, const unsigned ch
  * device resolves the array's device address (cudaGetSymbolAddress); make
  * that first call before any stream capture. All calls share the one array:
  * calls that can overlap on the GPU (different streams, or different host
- * threads on the same device) race and must be serialised by the caller. */
+ * threads on the same device) race and must be serialised by the caller.
+ * The resolved address is kept for the life of the process, so the library
+ * must not be used on a device after cudaDeviceReset or any other teardown of
+ * its primary context. */
 int msn_iuwt_decompose_static(const float *d_in, float *d_detail, float *d_smoothed, int ny, int nx,
                               int scale_count, int scale_adjust, void *stream);
 
@@ -241,6 +244,12 @@ int msn_dot2(const float *d_a, const float *d_b, const float *d_c, const float *
  * snr_ratio, pymoresane/iuwt_toolbox.py:292-306. */
 int msn_snr_sums(const float *d_a, const float *d_b, size_t n, double *d_out2, void *d_work, size_t work_bytes,
                  void *stream);
+
+/* The same two sums for float64 inputs, accumulated entirely in float64:
+ * snr_ratio of float64 arrays (pymoresane/iuwt_toolbox.py:292-306, whose
+ * np.linalg.norm reduces in the arrays' own float64). */
+int msn_snr_sums_f64(const double *d_a, const double *d_b, size_t n, double *d_out2, void *d_work,
+                     size_t work_bytes, void *stream);
 
 /* Running model sources for the minor-loop SNR (pymoresane/main.py:413-424):
  * ms += alpha * q (float32, alpha = (float)scal[2]) where q = mask * W(H p) is

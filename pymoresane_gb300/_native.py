@@ -54,6 +54,7 @@ SIGNATURES = {
     "msn_reduce_workspace_bytes": (c_size_t, []),
     "msn_dot2": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_size_t, c_void_p, c_void_p, c_size_t, c_void_p]),
     "msn_snr_sums": (c_int, [c_void_p, c_void_p, c_size_t, c_void_p, c_void_p, c_size_t, c_void_p]),
+    "msn_snr_sums_f64": (c_int, [c_void_p, c_void_p, c_size_t, c_void_p, c_void_p, c_size_t, c_void_p]),
     "msn_snr_update": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_size_t, c_void_p, c_void_p, c_size_t,
                                c_void_p]),
     "msn_segment_flags_bytes": (c_size_t, [c_size_t]),

@@ -118,9 +118,15 @@ class MemoryGate:
         if nbytes > self.budget:
             raise MemoryError(f"job needs {nbytes} bytes, more than the whole budget of {self.budget}")
         with self._cv:
-            if self.used + nbytes > self.budget and shrink is not None:
-                self.used -= shrink()
+            short = self.used + nbytes > self.budget
+        if short and shrink is not None:
+            # shrink() can take a while (it may empty torch's cache): run it without the
+            # lock so the other workers' acquire / release calls are not held up.
+            freed = shrink()
+            with self._cv:
+                self.used -= freed
                 self._cv.notify_all()
+        with self._cv:
             ok = self._cv.wait_for(lambda: self.used + nbytes <= self.budget, timeout)
             if not ok:
                 raise TimeoutError("no device memory became free for the job")

@@ -120,6 +120,21 @@ dual_partials(const float4 *__restrict__ a, const float4 *__restrict__ b, const 
     finish_pairs(s0, s1, partials, out, nullptr);
 }
 
+// Float64 inputs: partials of sum a^2 and sum (a - b)^2 with every product and
+// difference in float64 (np.linalg.norm of float64 arrays, iuwt_toolbox.py:304).
+__global__ void __launch_bounds__(kRedThreads)
+snr_partials_f64(const double *__restrict__ a, const double *__restrict__ b, size_t n,
+                 double *__restrict__ partials, double *__restrict__ out) {
+    double s0 = 0.0, s1 = 0.0;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const double va = __ldg(a + i);
+        const double d = __dsub_rn(va, __ldg(b + i));
+        s0 = __fma_rn(va, va, s0);
+        s1 = __fma_rn(d, d, s1);
+    }
+    finish_pairs(s0, s1, partials, out, nullptr);
+}
+
 // Sums the kRedGrid partial pairs in a fixed order into out[0], out[1]: one
 // warp-shuffle tree per warp, then one over the warp sums.
 constexpr int kFinalizeThreads = ((kRedGrid + 31) / 32) * 32;
@@ -410,6 +425,15 @@ extern "C" int msn_snr_sums(const float *d_a, const float *d_b, size_t n, double
     MSN_TRY(check_red_ws(d_work, work_bytes, "msn_snr_sums"));
     // out[0] = sum a^2, out[1] = sum (a - b)^2
     return dual_reduce(d_a, d_a, d_b, nullptr, n, true, d_out2, (double *)d_work, as_stream(stream));
+}
+
+extern "C" int msn_snr_sums_f64(const double *d_a, const double *d_b, size_t n, double *d_out2, void *d_work,
+                                size_t work_bytes, void *stream) {
+    clear_error();
+    if (!d_a || !d_b || !d_out2) return set_error(MSN_ERR_INVALID, "msn_snr_sums_f64: null pointer");
+    MSN_TRY(check_red_ws(d_work, work_bytes, "msn_snr_sums_f64"));
+    snr_partials_f64<<<kRedGrid, kRedThreads, 0, as_stream(stream)>>>(d_a, d_b, n, (double *)d_work, d_out2);
+    return check_launch("snr_partials_f64");
 }
 
 extern "C" int msn_snr_update(const float *d_e, float *d_ms, const float *d_q, const double *d_scal, size_t n,

@@ -342,6 +342,15 @@ def snr_sums(a, b, out=None, work=None):
     return out
 
 
+def snr_sums_f64(a, b, out=None, work=None):
+    """sum a^2, sum (a - b)^2 of two contiguous float64 CUDA tensors, all in float64."""
+    out = torch.empty(2, dtype=torch.float64, device=a.device) if out is None else out
+    work = reduce_workspace(a.device) if work is None else work
+    _native.call("msn_snr_sums_f64", a.data_ptr(), b.data_ptr(), a.numel(), out.data_ptr(), work.data_ptr(),
+                 work.numel(), stream_handle())
+    return out
+
+
 def mul(a, b, out):
     _native.call("msn_mul", a.data_ptr(), b.data_ptr(), out.data_ptr(), a.numel(), stream_handle())
     return out

@@ -6,7 +6,7 @@ as float32 and results come back as float32 numpy arrays; CUDA tensors are
 accepted as inputs (the reference accepts pycuda gpuarrays,
 pymoresane/iuwt.py:428-431) and ``store_on_gpu=True`` returns CUDA tensors.
 
-Differences from the reference, all documented in INTEGRATION.md:
+Differences from the reference:
 * only mode='gpu' is implemented; 'ser' and 'mp' raise ValueError (this
   package is the GPU path and has no CPU implementation);
 * with store_on_gpu=True and store_smoothed=True the smoothed plane is

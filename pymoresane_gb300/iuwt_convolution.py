@@ -10,7 +10,7 @@ with the 1/M^2 scale, fft-shift and centre crop folded in).
 (CUDA tensor or numpy array, e.g. from gpu_r2c_fft), which is converted to the
 packed layout on every call.
 
-Differences from the reference (documented in INTEGRATION.md): only
+Differences from the reference: only
 conv_device='gpu' is implemented; pad_array stays a host (numpy) helper as
 in the reference; device arrays are torch CUDA tensors.
 """

@@ -59,8 +59,32 @@ def source_extraction(in1, tolerance, mode="gpu", store_on_gpu=False, neg_comp=F
     return sources, _host(mask).astype(np.int32)
 
 
+def _is_f64(x):
+    if isinstance(x, torch.Tensor):
+        return x.dtype == torch.float64
+    return np.asarray(x).dtype == np.float64
+
+
+def _as_f64_cuda(x, device=None):
+    if isinstance(x, torch.Tensor):
+        t = x.to(device or (x.device if x.is_cuda else "cuda"))
+        return t.to(torch.float64).contiguous()
+    return torch.as_tensor(np.ascontiguousarray(x, dtype=np.float64)).to(device or "cuda")
+
+
 def snr_ratio(in1, in2):
-    """20 log10(||in1|| / ||in1 - in2||) with float64 device reductions."""
+    """20 log10(||in1|| / ||in1 - in2||) with float64 device reductions.
+
+    As np.linalg.norm in the reference (pymoresane/iuwt_toolbox.py:304), the
+    arithmetic follows the inputs' type: if either input is float64 the
+    difference and both norms are formed in float64; float32 inputs form
+    four-element float32 partials accumulated in float64.
+    """
+    if _is_f64(in1) or _is_f64(in2):
+        a = _as_f64_cuda(in1)
+        b = _as_f64_cuda(in2, device=a.device)
+        sums = _host(dev.snr_sums_f64(a.reshape(-1), b.reshape(-1)))
+        return float(20 * np.log10(np.sqrt(sums[0]) / np.sqrt(sums[1])))
     a = dev.as_f32_cuda(in1)
     b = dev.as_f32_cuda(in2, device=a.device)
     sums = _host(dev.snr_sums(a.reshape(-1), b.reshape(-1)))

@@ -11,7 +11,7 @@ products and step sizes are float64, the bulk arithmetic float32.
 
 Signatures and defaults follow the reference except that the mode arguments
 default to the GPU path ('gpu'); CPU modes raise ValueError (this package
-has no CPU implementation). See INTEGRATION.md for every difference.
+has no CPU implementation).
 """
 import ctypes
 import logging

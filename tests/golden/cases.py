@@ -42,3 +42,44 @@ def restore_inputs():
         residual = (0.01 * rng.standard_normal((n, n))).astype(np.float32)
         cases[tag] = (ptag, model, residual)
     return psfs, cases
+
+
+# Benchmark-size problems run end to end by the reference (make_golden.py
+# gen_baseline_*): the 512^2 problem with its full run parameters, and the
+# 2048^2 problem that bench.py times, bounded to a few major iterations and
+# also run to completion.
+BASELINE_RUN = dict(scale_count=5, sigma_level=4, loop_gain=0.2, tolerance=0.75, accuracy=1e-6,
+                    major_loop_miter=100, minor_loop_miter=30, conv_mode="linear")
+BASELINE_2048_RUN = dict(BASELINE_RUN, scale_count=7)
+
+
+def parse_major_log(lines):
+    """Per-major-iteration records from the INFO log lines of a MORESANE run.
+
+    Works on the reference's log text (pymoresane/main.py:316-507) and on this
+    package's identical text. Each record: the list of maximum scales and
+    minor-loop counts of the minor loops run in that major iteration (more
+    than one when the minimum scale is incremented), the last 'Scale k is
+    empty' adjust, and whether the step was reverted.
+    """
+    recs, cur = [], None
+
+    def fresh():
+        return {"max_scale": [], "minor": [], "scale_adjust": [], "reverted": False}
+
+    for ln in lines:
+        if cur is None:
+            cur = fresh()
+        if ln.startswith("Maximum scale = "):
+            cur["max_scale"].append(int(ln.split("=")[1]))
+            cur["scale_adjust"].append(0)
+        elif ln.startswith("Scale ") and " is empty." in ln:
+            cur["scale_adjust"][-1] = int(ln.split()[1])
+        elif ln.endswith("minor loop iterations performed."):
+            cur["minor"].append(int(ln.split()[0]))
+        elif ln.startswith("Residual has worsened"):
+            cur["reverted"] = True
+        elif ln.endswith("major loop iterations performed."):
+            recs.append(cur)
+            cur = None
+    return recs

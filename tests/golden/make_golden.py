@@ -11,8 +11,11 @@ Run from the repository root in a checkout where the reference sources exist:
 The GPU machine never runs this script; it only reads the committed fixtures.
 """
 import argparse
+import hashlib
+import logging
 import os
 import sys
+import time
 
 import numpy as np
 
@@ -21,7 +24,8 @@ sys.path.insert(0, HERE)
 sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
 
 import refshim  # noqa: E402
-from cases import MORESANE_CASES, RUN_DEFAULTS, problem, restore_inputs  # noqa: E402
+from cases import (BASELINE_2048_RUN, BASELINE_RUN, MORESANE_CASES, RUN_DEFAULTS,  # noqa: E402
+                   parse_major_log, problem, restore_inputs)
 
 
 def save(name, **arrays):
@@ -148,8 +152,90 @@ def gen_restore(ref):
     save("restore", **out)
 
 
+class _InfoLines(logging.Handler):
+    """Collects the INFO messages of the reference's logger (pymoresane/main.py:15)."""
+
+    def __init__(self):
+        super().__init__(logging.INFO)
+        self.lines = []
+
+    def emit(self, record):
+        self.lines.append(record.getMessage())
+
+
+def digest(a):
+    """sha256 of an array's bytes, as uint8 (pins regenerated inputs to the ones used here)."""
+    return np.frombuffer(hashlib.sha256(np.ascontiguousarray(a).tobytes()).digest(), np.uint8)
+
+
+def run_logged(ref, dirty, psf, kw):
+    """DataImage.moresane of the reference with its INFO log captured; returns (img, lines, seconds)."""
+    lg = logging.getLogger(ref.main.__name__)
+    h = _InfoLines()
+    lg.addHandler(h)
+    old = lg.level
+    lg.setLevel(logging.INFO)
+    try:
+        img = ref.main.DataImage(dirty, psf, None, 1.0, 1.0)
+        t0 = time.perf_counter()
+        img.moresane(subregion=dirty.shape[0], **kw)
+        dt = time.perf_counter() - t0
+    finally:
+        lg.removeHandler(h)
+        lg.setLevel(old)
+    return img, h.lines, dt
+
+
+def save_baseline(name, dirty, psf, kw, img, lines, dt, full_residual):
+    """Sparse model, residual (whole or a 256^2 centre crop + std), log text and run time."""
+    recs = parse_major_log(lines)
+    flat = img.model.ravel()
+    idx = np.flatnonzero(flat).astype(np.int64)
+    n = dirty.shape[0]
+    c = slice(n // 2 - 128, n // 2 + 128)
+    out = dict(dirty_sha=digest(dirty), psf_sha=digest(psf), model_idx=idx, model_val=flat[idx],
+               model_shape=np.array(img.model.shape), residual_std=np.array(np.std(img.residual)),
+               residual_centre=img.residual[c, c], log=np.array(lines), seconds=np.array(dt),
+               major=np.array(len(recs)), minor_total=np.array(sum(sum(r["minor"]) for r in recs)),
+               major_loop_miter=np.array(kw["major_loop_miter"]))
+    if full_residual:
+        out["residual"] = img.residual
+    print(name, "major", len(recs), "minor", int(out["minor_total"]), "seconds", round(dt, 1),
+          "model nnz", idx.size, "residual std", float(out["residual_std"]))
+    save(name, **out)
+
+
+def gen_baseline_512(ref):
+    """The 512^2 problem (1024^2 PSF, 3000 uv points) with its full run parameters, linear."""
+    from pymoresane_gb300 import synthetic
+    dirty, psf, _ = synthetic.make_problem(synthetic.problem_512(0))
+    img, lines, dt = run_logged(ref, dirty, psf, dict(BASELINE_RUN))
+    save_baseline("baseline_512", dirty, psf, BASELINE_RUN, img, lines, dt, full_residual=True)
+
+
+def _gen_2048(ref, name, miter):
+    from pymoresane_gb300 import synthetic
+    dirty, psf, _ = synthetic.make_problem(synthetic.problem_2048(0))
+    kw = dict(BASELINE_2048_RUN, major_loop_miter=miter)
+    img, lines, dt = run_logged(ref, dirty, psf, kw)
+    save_baseline(name, dirty, psf, kw, img, lines, dt, full_residual=False)
+
+
+def gen_baseline_2048_m3(ref):
+    """The 2048^2 problem (4096^2 PSF, 20000 uv points, S=7) bounded to 3 major iterations."""
+    _gen_2048(ref, "baseline_2048_m3", 3)
+
+
+def gen_baseline_2048_full(ref):
+    """The same 2048^2 problem run to completion (hours on one core)."""
+    _gen_2048(ref, "baseline_2048_full", BASELINE_2048_RUN["major_loop_miter"])
+
+
 GENERATORS = {"restore": gen_restore, "iuwt": gen_iuwt, "conv": gen_conv, "toolbox": gen_toolbox, "moresane": gen_moresane,
-              "tart": gen_tart}
+              "tart": gen_tart, "baseline_512": gen_baseline_512, "baseline_2048_m3": gen_baseline_2048_m3,
+              "baseline_2048_full": gen_baseline_2048_full}
+# slow: run only when named with --only
+SLOW = {"baseline_512", "baseline_2048_m3", "baseline_2048_full"}
 
 
 def main():
@@ -158,7 +244,7 @@ def main():
     args = ap.parse_args()
     ref = refshim.load_reference()
     for name, fn in GENERATORS.items():
-        if args.only and name not in args.only:
+        if (args.only and name not in args.only) or (not args.only and name in SLOW):
             continue
         fn(ref)
 

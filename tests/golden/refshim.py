@@ -29,7 +29,8 @@ import sys
 import types
 import contextlib
 
-REF_ROOT = os.environ.get("PYMORESANE_REF", "/root/reference")
+# Root of a reference PyMORESANE checkout (the directory holding pymoresane/); required.
+REF_ROOT = os.environ.get("PYMORESANE_REF", "")
 
 
 def _patch(name, src):
@@ -50,6 +51,8 @@ def _patch(name, src):
 
 def load_reference():
     """Return the patched reference package ``pymoresane`` (a module object)."""
+    if not REF_ROOT or not os.path.isdir(os.path.join(REF_ROOT, "pymoresane")):
+        raise RuntimeError("set PYMORESANE_REF to the root of a reference PyMORESANE checkout")
     if "pymoresane" in sys.modules and getattr(sys.modules["pymoresane"], "_shimmed", False):
         return sys.modules["pymoresane"]
     pylab = types.ModuleType("pylab")

@@ -102,3 +102,19 @@ def test_snr_ratio():
     from oracle import toolbox as T
     g = load("toolbox")
     assert T.snr_ratio(g["thresh"][1:4].astype(np.float64), g["decomp"][1:4]) == float(g["snr"])
+
+
+@pytest.mark.parametrize("name", ["lin_double", "circ_pos", "lin_same_edge", "lin_subregion", "neg_excl"])
+def test_moresane_oracle_bit_exact(name):
+    """oracle/moresane.py (precision='ref') reproduces the reference's own runs bit for bit."""
+    import sys
+    sys.path.insert(0, GOLDEN)
+    import cases as mg
+    from oracle.moresane import MoresaneOracle
+    g = load("moresane")
+    kw = dict(mg.RUN_DEFAULTS, **mg.MORESANE_CASES[name][1])
+    o = MoresaneOracle(g[f"{name}_dirty"], g[f"{name}_psf"], precision="ref")
+    o.moresane(**kw)
+    assert o.model.dtype == g[f"{name}_model"].dtype
+    assert np.array_equal(o.model, g[f"{name}_model"])
+    assert np.array_equal(o.residual, g[f"{name}_residual"])

@@ -130,6 +130,16 @@ def test_snr_ratio(cuda):
     assert abs(G.snr_ratio(a, b) - T.snr_ratio(a.astype(np.float64), b)) <= 1e-6 * abs(T.snr_ratio(a, b))
 
 
+def test_snr_ratio_float64_inputs(cuda):
+    # float64 inputs reduce in float64 (np.linalg.norm, iuwt_toolbox.py:304): the reference's golden value
+    g = golden()
+    a = g["thresh"][1:4].astype(np.float64)
+    b = g["decomp"][1:4]
+    want = float(g["snr"])
+    assert abs(G.snr_ratio(a, b) - want) <= 1e-12 * abs(want)
+    assert abs(G.snr_ratio(torch.as_tensor(a).cuda(), torch.as_tensor(b).cuda()) - want) <= 1e-12 * abs(want)
+
+
 def test_cg_vector_kernels(cuda):
     from pymoresane_gb300 import _native
     rng = np.random.default_rng(5)

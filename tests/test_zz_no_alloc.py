@@ -29,10 +29,21 @@ def decompose_static(x, scale_count, scale_adjust):
     ny, nx = x.shape
     detail = torch.empty((scale_count - scale_adjust, ny, nx), dtype=torch.float32, device=x.device)
     smoothed = torch.empty((ny, nx), dtype=torch.float32, device=x.device)
+    args = ("msn_iuwt_decompose_static", x.data_ptr(), detail.data_ptr(), smoothed.data_ptr(), ny, nx,
+            scale_count, scale_adjust, torch.cuda.current_stream().cuda_stream)
+    # A first call with these arguments loads the kernels it uses: with lazy module
+    # loading the driver may reserve device memory for them (and for the static array)
+    # at that point. The call after it is the one checked.
+    _native.call(*args)
+    # torch's allocator counter sees allocations made through torch; the device's free
+    # memory (cudaMemGetInfo) also sees a cudaMalloc made inside libmsn.so itself.
+    torch.cuda.synchronize()
     before = torch.cuda.memory_allocated()
-    _native.call("msn_iuwt_decompose_static", x.data_ptr(), detail.data_ptr(), smoothed.data_ptr(), ny, nx,
-                 scale_count, scale_adjust, torch.cuda.current_stream().cuda_stream)
+    free_before = torch.cuda.mem_get_info()[0]
+    _native.call(*args)
+    torch.cuda.synchronize()
     assert torch.cuda.memory_allocated() == before
+    assert torch.cuda.mem_get_info()[0] == free_before
     return detail, smoothed
 
 
