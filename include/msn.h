@@ -157,6 +157,11 @@ int msn_spectrum_pack(const void *d_std, int m, void *d_packed, void *stream);
 int msn_fft_convolve(const float *d_x, int n, int m, const void *d_spec, float *d_out, int linear, void *d_work,
                      size_t work_bytes, void *stream);
 
+/* Reads and clears the status word of the persistent FFT kernels (synchronous):
+ * bit 0 is set when a bounded wait for a bulk copy gave up, in which case the
+ * convolution's output is not valid. No counterpart in the reference. */
+int msn_fft_status(unsigned *out);
+
 /* Replaces gpu_r2c_fft -- pymoresane/iuwt_convolution.py:76-106:
  * d_out [m][m/2+1] = rfft2(d_in [m][m]). */
 int msn_rfft2(const float *d_in, int m, void *d_out, void *d_work, size_t work_bytes, void *stream);

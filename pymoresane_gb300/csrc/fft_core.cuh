@@ -44,28 +44,28 @@ __device__ __forceinline__ void cp_async_wait() {
     asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
 }
 
-__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
-__device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
-__device__ __forceinline__ float2 cmul(float2 a, float2 b) {
+__host__ __device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__host__ __device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+__host__ __device__ __forceinline__ float2 cmul(float2 a, float2 b) {
     return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
-__device__ __forceinline__ float2 cconj(float2 a) { return make_float2(a.x, -a.y); }
+__host__ __device__ __forceinline__ float2 cconj(float2 a) { return make_float2(a.x, -a.y); }
 
 // Multiply by -i (forward) or +i (inverse).
 template <bool INV>
-__device__ __forceinline__ float2 rot90(float2 a) {
+__host__ __device__ __forceinline__ float2 rot90(float2 a) {
     return INV ? make_float2(-a.y, a.x) : make_float2(a.y, -a.x);
 }
 
 template <bool INV>
-__device__ __forceinline__ void dft2(float2 *v) {
+__host__ __device__ __forceinline__ void dft2(float2 *v) {
     const float2 a = v[0], b = v[1];
     v[0] = cadd(a, b);
     v[1] = csub(a, b);
 }
 
 template <bool INV>
-__device__ __forceinline__ void dft3(float2 *v) {
+__host__ __device__ __forceinline__ void dft3(float2 *v) {
     const float s = INV ? 0.86602540378443864676f : -0.86602540378443864676f;
     const float2 a = v[0], b = v[1], c = v[2];
     const float2 t1 = cadd(b, c);
@@ -79,7 +79,7 @@ __device__ __forceinline__ void dft3(float2 *v) {
 
 // 4-point DFT of v[o], v[o+s], v[o+2s], v[o+3s] in place, natural order.
 template <bool INV, int O, int S>
-__device__ __forceinline__ void dft4s(float2 *v) {
+__host__ __device__ __forceinline__ void dft4s(float2 *v) {
     const float2 x0 = v[O], x1 = v[O + S], x2 = v[O + 2 * S], x3 = v[O + 3 * S];
     const float2 a0 = cadd(x0, x2), a1 = csub(x0, x2), a2 = cadd(x1, x3), a3 = rot90<INV>(csub(x1, x3));
     v[O] = cadd(a0, a2);
@@ -89,12 +89,12 @@ __device__ __forceinline__ void dft4s(float2 *v) {
 }
 
 template <bool INV>
-__device__ __forceinline__ void dft4(float2 *v) {
+__host__ __device__ __forceinline__ void dft4(float2 *v) {
     dft4s<INV, 0, 1>(v);
 }
 
 template <bool INV>
-__device__ __forceinline__ void dft8(float2 *v) {
+__host__ __device__ __forceinline__ void dft8(float2 *v) {
     // X[k] = E[k] + w8^k O[k], X[k+4] = E[k] - w8^k O[k].
     float2 e[4] = {v[0], v[2], v[4], v[6]};
     float2 o[4] = {v[1], v[3], v[5], v[7]};
@@ -117,7 +117,7 @@ __device__ __forceinline__ void dft8(float2 *v) {
 }
 
 template <bool INV>
-__device__ __forceinline__ void dft16(float2 *v) {
+__host__ __device__ __forceinline__ void dft16(float2 *v) {
     // 4 x 4: n = 4 n1 + n2, k = k1 + 4 k2.
     dft4s<INV, 0, 4>(v);
     dft4s<INV, 1, 4>(v);
@@ -152,7 +152,7 @@ __host__ __device__ constexpr int out_slot(int r) {
 }
 
 template <bool INV, int R>
-__device__ __forceinline__ void dft(float2 *v) {
+__host__ __device__ __forceinline__ void dft(float2 *v) {
     if constexpr (R == 2) dft2<INV>(v);
     if constexpr (R == 3) dft3<INV>(v);
     if constexpr (R == 4) dft4<INV>(v);
@@ -160,8 +160,10 @@ __device__ __forceinline__ void dft(float2 *v) {
     if constexpr (R == 16) dft16<INV>(v);
 }
 
+#ifndef MSN_HOST_ONLY  // host-only test programs compile the arithmetic without the device table
 static __device__ const float2 kTwiddle[kTwN] = {
 #include "msn_twiddles.inc"
 };
+#endif
 
 }  // namespace msn

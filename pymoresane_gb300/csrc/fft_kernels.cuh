@@ -699,6 +699,10 @@ int launch_cols(const float2 *in, InL in_lay, int in_rows, int in_off, const flo
 template <int M>
 int conv_run(const float *x, int n, const float2 *spec, float *out, int linear, float2 *t1, float2 *t2,
              cudaStream_t st) {
+    if constexpr (M == sq::kLength) {
+        // the 2048^2 linear convolution with a 4096^2 PSF: four-step kernels
+        if (linear && n == M / 2) return sq::conv_run(x, spec, out, t1, t2, st);
+    }
     const int off = linear ? (M - n) / 2 : 0;
     const int shift = (off + M / 2) % M;
     const float div = (float)M * (float)M;

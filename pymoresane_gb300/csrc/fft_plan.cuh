@@ -92,6 +92,14 @@ int rfft2_run(const float *in, float2 *out, float2 *t1, cudaStream_t st);
 template <int M>
 int irfft2_run(const float2 *in, float *out, float2 *t2, cudaStream_t st);
 
+namespace sq {
+// Linear convolution of a 2048^2 image with a 4096^2 PSF spectrum (packed,
+// group-major with 2 columns per group) by the four-step kernels of
+// fft_sq.cuh; lo / hi: two workspaces of kPlaneElems float2 each.
+constexpr int kLength = 4096;
+int conv_run(const float *x, const float2 *spec, float *out, float2 *lo, float2 *hi, cudaStream_t st);
+}  // namespace sq
+
 #define MSN_FFT_SIZES(X) \
     X(24) X(48) X(96) X(192) X(384) X(768) X(1536) X(3072) X(6144) \
     X(32) X(64) X(128) X(256) X(512) X(1024) X(2048) X(4096) X(8192)

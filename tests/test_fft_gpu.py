@@ -121,3 +121,19 @@ def test_full_size_convolution_2048_linear(cuda):
     s = dev.fft_convolve(torch.from_numpy(x + y).cuda(), spec)
     a = dev.fft_convolve(torch.from_numpy(x).cuda(), spec) + dev.fft_convolve(torch.from_numpy(y).cuda(), spec)
     assert torch.max(torch.abs(s - a)).item() <= 1e-5 * torch.max(torch.abs(s)).item()
+    # the persistent kernels' bounded waits never gave up
+    import ctypes
+    from pymoresane_gb300 import _native
+    status = ctypes.c_uint(99)
+    _native.call("msn_fft_status", ctypes.byref(status))
+    assert status.value == 0
+
+
+def test_full_size_convolution_2048_dense_random(cuda):
+    # dense random image and PSF through the four-step 4096-point path, against float64 numpy
+    rng = np.random.default_rng(4096)
+    psf = rng.random((4096, 4096)).astype(np.float32)
+    x = rng.standard_normal((2048, 2048)).astype(np.float32)
+    ref = OC.fft_convolve(x.astype(np.float64), np.fft.rfft2(psf.astype(np.float64)), "linear")
+    got = G.fft_convolve(x, dev.psf_spectrum(psf), "gpu", "linear")
+    assert np.max(np.abs(got - ref)) <= CONV_TOL * np.max(np.abs(ref))
