@@ -39,11 +39,28 @@ PEAKS_PATH = os.path.join(ROOT, "MEASURED_PEAKS.json")
 FALLBACK_HBM_GBS = 6800.0
 DECONV_KW = dict(scale_count=7, sigma_level=4, loop_gain=0.2, tolerance=0.75, accuracy=1e-6, major_loop_miter=100,
                  minor_loop_miter=30, conv_mode="linear")
-# Trajectory of the seed-0 2048^2 workload (major, minor iterations) as run by this
-# implementation on a GB300; used only to scale the CPU samples of the reference
-# arm, which cannot run a whole deconvolution in minutes.
-DECONV_TRAJECTORY = (90, 1419)
 IUWT_N, IUWT_S = 4096, 8
+# The workload names and L2 notes both arms print in "config" (the same dict in each arm).
+CONFIGS = {
+    "deconv": {"workload": "moresane_2048x2048_psf4096_S7_linear",
+               "l2": "working set > 0.6 GB per deconvolution > 129 MB L2 (no flush needed)"},
+    "iuwt": {"workload": "iuwt_4096x4096_S8_store_smoothed",
+             "l2": "working set 0.7 GB per step > 129 MB L2 (no flush needed)"},
+}
+
+
+def reference_trajectory():
+    """(major, minor) iterations of the reference's own complete run of the 2048^2 problem.
+
+    Read from the fixture tests/golden/baseline_2048_full.npz, made by running
+    the reference PyMORESANE on the same seeded problem (tests/golden/make_golden.py);
+    None when the fixture is absent.
+    """
+    path = os.path.join(ROOT, "tests", "golden", "baseline_2048_full.npz")
+    if not os.path.exists(path):
+        return None
+    g = np.load(path)
+    return int(g["major"]), int(g["minor_total"])
 
 
 def load_peaks():
@@ -232,28 +249,37 @@ def deconv_problem(seed):
     return dirty, psf
 
 
-def cpu_deconv(dirty, psf, decom, workers, trajectory):
+def cpu_deconv(dirty, psf, decom, workers, trajectory, source):
     """Oracle port of the reference MORESANE timed on a bounded sample, scaled to one deconvolution.
 
-    The sample is the set-up (PSF spectra and energies) plus the first major
-    iteration with its first two minor iterations; the per-major and
-    per-minor times are scaled by the trajectory (major, minor) of a full run.
+    The sample is the set-up (PSF spectra and energies) plus the whole first
+    major iteration with all of its minor iterations; the per-major and
+    per-minor times are scaled by the trajectory (major, minor) of a complete
+    run, whose origin `source` names.
     """
     from oracle.moresane import MoresaneOracle
     o = MoresaneOracle(dirty, psf, decom=decom, workers=workers)
     t0 = time.perf_counter()
-    o.moresane(**dict(DECONV_KW, major_loop_miter=1, minor_loop_miter=2))
+    o.moresane(**dict(DECONV_KW, major_loop_miter=1))
     wall = time.perf_counter() - t0
     t = o.timings
     per_major = t["major"] / max(1, t["n_major"])
     per_minor = t["minor"] / max(1, t["n_minor"])
     n_major, n_minor = trajectory
     seconds = t["setup"] + n_major * per_major + n_minor * per_minor
-    sample = (f"2048^2 config: set-up + 1 major + {t['n_minor']} minor iterations of the oracle port "
-              f"({'FP64 ser' if decom == 'ser' else 'FP32 mp'} IUWT, numpy FFT, scipy labelling) in {wall:.1f} s, "
-              f"scaled to a full deconvolution of {n_major} major / {n_minor} minor iterations "
-              f"(per major {per_major:.2f} s, per minor {per_minor:.2f} s)")
+    sample = (f"2048^2 problem: set-up + the first major iteration with all {t['n_minor']} of its minor iterations "
+              f"of the oracle port ({'FP64 ser' if decom == 'ser' else 'FP32 mp'} IUWT, numpy FFT, scipy "
+              f"labelling) in {wall:.1f} s on {workers} thread(s), scaled to {source}: {n_major} major / "
+              f"{n_minor} minor iterations (per major {per_major:.2f} s, per minor {per_minor:.2f} s)")
     return 1.0 / seconds, sample
+
+
+def deconv_trajectory(fallback):
+    """The reference's own trajectory when its fixture exists, else the GPU run's (named)."""
+    ref = reference_trajectory()
+    if ref is not None:
+        return ref, "the reference's own complete run of this problem"
+    return tuple(fallback), "this implementation's complete run of this problem (reference run not recorded)"
 
 
 def run_deconv(args, rank, world, dist):
@@ -503,22 +529,32 @@ def main():
         if rank != 0:
             return
         workers = os.cpu_count() or 1
-        vals, sample = [], None
+        vals, sample, traj = [], None, None
         if args.workload == "deconv":
             dirty, psf = deconv_problem(0)
+            ref = reference_trajectory()
+            traj, source = (ref, "the reference's own complete run of this problem") if ref else \
+                ((90, 1409), "this implementation's complete run of this problem on GB300 (reference run not recorded)")
+        # Each step is a bounded sample of seconds; warm-up samples are untimed. The run stops
+        # taking samples after about 150 s (at least one timed sample), so that it ends in minutes.
+        t_run = time.perf_counter()
         for i in range(args.warmup + args.steps):
             if args.workload == "deconv":
-                v, sample = cpu_deconv(dirty, psf, "mp", workers, DECONV_TRAJECTORY)
+                v, sample = cpu_deconv(dirty, psf, "mp", workers, traj, source)
             else:
                 v, sample = cpu_iuwt(workers)
             if i >= args.warmup:
                 vals.append(v)
+            if vals and time.perf_counter() - t_run > 150.0:
+                break
         value = statistics.mean(vals)
+        sample = f"{sample}; mean of {len(vals)} timed sample(s)"
+        extra = {"trajectory_major_minor": list(traj)} if traj else {}
         print(json.dumps({
             "impl": "reference", "metric": metric, "value": value, "unit": unit, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": args.workload, "parallelism": f"host, {workers} threads"},
+            "config": dict(CONFIGS[args.workload]), "parallelism": f"host, {workers} threads", **extra,
             "cpu_baseline": {"value": value, "unit": unit, "cores": workers, "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         }))
@@ -603,11 +639,11 @@ def main():
                 "metric": metric, "value": world * alg / (ms * 1e-3) / 1e9, "unit": unit, "n_gpus": world,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-                "config": {"workload": "iuwt_4096x4096_S8_store_smoothed",
-                           "l2": "working set 0.7 GB per step > 129 MB L2 (no flush needed)",
-                           "parallelism": f"replicas x{world}"},
-                "roofline": {"bound": "hbm", "kernel": "atrous_band", "achieved": r["kernel_gbs"], "peak": hbm_peak,
-                             "peak_kind": peak_kind, "unit": "GB/s", "frac": r["kernel_gbs"] / hbm_peak,
+                "config": dict(CONFIGS["iuwt"]), "parallelism": f"replicas x{world}",
+                "roofline": {"bound": "hbm", "kernel": "IUWT decomposition + recomposition (all passes)",
+                             "achieved": r["gbs"], "peak": hbm_peak, "peak_kind": peak_kind, "unit": "GB/s",
+                             "frac": r["gbs"] / hbm_peak, "bytes": "algorithmic: 4 N^2 (1 + S + 1) + 4 N^2 (S + 1 + 1)",
+                             "per_pass_gbs": r["kernel_gbs"],
                              "traffic": (read_traffic("iuwt_traffic.json") or {}).get("bytes_per_launch")},
                 "e2e": {"value": world * alg / e2e_s / 1e9, "unit": "GB/s", "h2d_bytes_per_step": 4 * n * n * (s + 2),
                         "d2h_bytes_per_step": 4 * n * n * (s + 2)},
@@ -629,7 +665,8 @@ def main():
     if rank == 0:
         cpu = None
         if not args.no_cpu_baseline:
-            v, sample = cpu_deconv(res["dirty"], res["psf"], "ser", 1, res["traj"])
+            traj, source = deconv_trajectory(res["traj"])
+            v, sample = cpu_deconv(res["dirty"], res["psf"], "ser", 1, traj, source)
             cpu = {"value": v, "unit": "deconv/s", "cores": 1, "kind": "port", "sample": sample}
         n = 2048
         m = 4096
@@ -637,10 +674,9 @@ def main():
             "metric": metric, "value": value, "unit": unit, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": "moresane_2048x2048_psf4096_S7_linear",
-                       "trajectory_major_minor": list(res["traj"]), "driver": args.driver,
-                       "l2": "working set > 0.6 GB per deconvolution > 129 MB L2 (no flush needed)",
-                       "parallelism": f"replicas x{world}"},
+            "config": dict(CONFIGS["deconv"]), "trajectory_major_minor": list(res["traj"]),
+            "reference_trajectory_major_minor": list(reference_trajectory() or []) or None,
+            "driver": args.driver, "parallelism": f"replicas x{world}",
             "latency_ms": {"p50": percentile(res["lat"], 50), "p99": percentile(res["lat"], 99),
                            "mode": "plain (one image at a time)"},
             "iuwt_gbs": iuwt["gbs"], "iuwt_frac_of_hbm": iuwt["gbs"] / hbm_peak,
