@@ -510,6 +510,7 @@ def main():
     ap.add_argument("--distinct", type=int, default=3, help="batch / serve: distinct problems per size")
     ap.add_argument("--served-jobs", type=int, default=8, help="deconv: jobs of the served 2048^2 measurement (0: skip)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-tune", action="store_true", help="skip the autotuner (use the current launch parameters)")
     ap.add_argument("--driver", default="native", choices=["native", "host"],
                     help="deconv: native = minor/major loops in libmsn (graphs); host = step by step (for ncu)")
     args = ap.parse_args()
@@ -624,6 +625,8 @@ def main():
             time.sleep(0.3)
         if dist:
             dist.barrier()
+        from pymoresane_gb300 import tune
+        tuned = tune.autotune(n=IUWT_N, reps=5)["values"] if not args.no_tune else tune.current()
         r = measure_iuwt(args.steps, args.warmup, seed=rank)
         ms = replicas.reduce_max([r["ms_per_step"]], dist, "cuda")[0]
         clocks = sampler.stop() if sampler else None
@@ -648,11 +651,15 @@ def main():
                 "e2e": {"value": world * alg / e2e_s / 1e9, "unit": "GB/s", "h2d_bytes_per_step": 4 * n * n * (s + 2),
                         "d2h_bytes_per_step": 4 * n * n * (s + 2)},
                 "gpu_launches": int(r["launches_per_step"] * args.steps), "clocks": clocks, "cpu_baseline": cpu,
+                "autotuned": tuned,
             }))
         if dist:
             dist.destroy_process_group()
         return
 
+    # the project's autotuner picks this device's launch parameters before anything is timed
+    from pymoresane_gb300 import tune
+    tuned = tune.autotune(n=2048, reps=5)["values"] if not args.no_tune else tune.current()
     res = run_deconv(args, rank, world, dist)
     served = None
     if args.served_jobs > 0 and args.driver == "native":
@@ -690,7 +697,7 @@ def main():
                     "d2h_bytes_per_step": 8 * n * n, "steps": res["e2e_steps"],
                     "api": "pymoresane_gb300.main.DataImage(dirty, psf).moresane(...) with host numpy arrays"},
             "gpu_launches": res["launches"], "clocks": res["clocks"], "cpu_baseline": cpu,
-            "served": served,
+            "served": served, "autotuned": tuned,
         }))
     if dist:
         dist.destroy_process_group()

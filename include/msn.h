@@ -240,6 +240,32 @@ int msn_label(const float *d_img, int ny, int nx, int *d_labels, int *d_count, v
  * (calls that overlap on the GPU must not share it). */
 size_t msn_reduce_workspace_bytes(void);
 
+/* Accumulation type of every reduction of the library (CG inner products,
+ * SNR norms, residual statistics), process-wide: 64 (float64 accumulation of
+ * float32 four-element partials, the default) or 32 (plain float32
+ * accumulation). The float32 setting exists to state the error of a plain
+ * float32 path against the float64 one; the reference's GPU path reduces on
+ * the host in its arrays' precision (pymoresane/main.py:386-411). Minor-loop
+ * graphs are cached per setting. Returns MSN_ERR_INVALID for other values. */
+int msn_set_reduction_precision(int bits);
+int msn_reduction_precision(void);
+
+/* Tunable launch parameters, chosen per device by the autotuner
+ * (pymoresane_gb300/tune.py) and read by every launch. Names and ranges:
+ *   fft_four_step    0 or 1: the 2048^2 linear convolution with a 4096^2 PSF
+ *                    runs on the four-step kernels (1) or the Stockham ones (0)
+ *   fft_sq_fwd_ctas, fft_sq_col_ctas, fft_sq_inv_ctas
+ *                    0..8: resident CTAs per SM of the three four-step kernels
+ *                    (0: as many as fit)
+ *   iuwt_threads     64, 128 or 256: threads per CTA of the a trous passes
+ * Results do not depend on them. Changing one invalidates cached minor-loop
+ * graphs. No counterpart in the reference (which fixes its launch shapes,
+ * 32 x 32 blocks, pymoresane/iuwt.py:452-460). */
+int msn_tune_set(const char *name, int value);
+int msn_tune_get(const char *name, int *value);
+int msn_tune_reset(void);
+unsigned msn_tune_epoch(void);
+
 /* d_out2[0] = sum a*b, d_out2[1] = sum c*d (c, d may both be NULL) in float64
  * (np.dot at pymoresane/main.py:386-387,407-408). */
 int msn_dot2(const float *d_a, const float *d_b, const float *d_c, const float *d_d, size_t n, double *d_out2,

@@ -53,6 +53,12 @@ SIGNATURES = {
     "msn_plane_max": (c_int, [c_void_p, c_int, c_size_t, c_int, c_void_p, c_void_p, c_size_t, c_void_p]),
     "msn_label": (c_int, [c_void_p, c_int, c_int, c_void_p, c_void_p, c_void_p, c_size_t, c_void_p]),
     "msn_reduce_workspace_bytes": (c_size_t, []),
+    "msn_set_reduction_precision": (c_int, [c_int]),
+    "msn_reduction_precision": (c_int, []),
+    "msn_tune_set": (c_int, [ctypes.c_char_p, c_int]),
+    "msn_tune_get": (c_int, [ctypes.c_char_p, c_void_p]),
+    "msn_tune_reset": (c_int, []),
+    "msn_tune_epoch": (ctypes.c_uint, []),
     "msn_dot2": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_size_t, c_void_p, c_void_p, c_size_t, c_void_p]),
     "msn_snr_sums": (c_int, [c_void_p, c_void_p, c_size_t, c_void_p, c_void_p, c_size_t, c_void_p]),
     "msn_snr_sums_f64": (c_int, [c_void_p, c_void_p, c_size_t, c_void_p, c_void_p, c_size_t, c_void_p]),

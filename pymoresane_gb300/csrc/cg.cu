@@ -9,6 +9,8 @@
 // not depend on what else shares the GPU. The CG scalars live in a small
 // device array (layout MSN_S_* in msn.h) so that the vector updates read
 // alpha and beta on the device and the host only needs the stop decisions.
+#include <atomic>
+
 #include "msn_common.cuh"
 
 namespace msn {
@@ -19,13 +21,17 @@ constexpr int kRedThreads = 256;
 
 enum { S_RR = 0, S_PAP = 1, S_ALPHA = 2, S_RNRN = 3, S_BETA = 4 };
 
-__device__ __forceinline__ double block_sum(double v) {
-    __shared__ double sh[32];
+// Accumulation type of the reductions: double (default) or float (the plain
+// float32 variant selected with msn_set_reduction_precision(32), kept for the
+// float32-versus-float64 error comparison).
+template <class T>
+__device__ __forceinline__ T block_sum(T v) {
+    __shared__ T sh[32];
     for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
     if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
     __syncthreads();
     const int nw = blockDim.x >> 5;
-    v = threadIdx.x < nw ? sh[threadIdx.x] : 0.0;
+    v = threadIdx.x < nw ? sh[threadIdx.x] : T(0);
     if (threadIdx.x < 32)
         for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
     __syncthreads();
@@ -37,10 +43,11 @@ __device__ __forceinline__ double block_sum(double v) {
 // partials, reset to zero by that CTA) sums the kRedGrid pairs in a fixed
 // order -- thread t adds pairs t, t + 256, t + 512, then warp-shuffle trees --
 // so the totals do not depend on which CTA finishes last.
-__device__ __forceinline__ bool finish_pairs(double s0, double s1, double *__restrict__ partials, double *out,
+template <class T>
+__device__ __forceinline__ bool finish_pairs(T s0, T s1, double *__restrict__ partials, double *out,
                                              double *beta_scal) {
     __shared__ bool last;
-    __shared__ double ws[2][kRedThreads / 32];
+    __shared__ T ws[2][kRedThreads / 32];
     s0 = block_sum(s0);
     s1 = block_sum(s1);
     unsigned *counter = reinterpret_cast<unsigned *>(partials + 2 * kRedGrid);
@@ -53,10 +60,10 @@ __device__ __forceinline__ bool finish_pairs(double s0, double s1, double *__res
     __syncthreads();
     if (!last) return false;
     const int t = threadIdx.x;
-    double a = 0.0, b = 0.0;
+    T a = T(0), b = T(0);
     for (int k = t; k < (int)gridDim.x; k += kRedThreads) {
-        a += __ldcg(partials + 2 * k);
-        b += __ldcg(partials + 2 * k + 1);
+        a += (T)__ldcg(partials + 2 * k);
+        b += (T)__ldcg(partials + 2 * k + 1);
     }
     for (int off = 16; off > 0; off >>= 1) {
         a += __shfl_xor_sync(0xffffffffu, a, off);
@@ -68,18 +75,18 @@ __device__ __forceinline__ bool finish_pairs(double s0, double s1, double *__res
     }
     __syncthreads();
     if (t < 32) {
-        a = t < kRedThreads / 32 ? ws[0][t] : 0.0;
-        b = t < kRedThreads / 32 ? ws[1][t] : 0.0;
+        a = t < kRedThreads / 32 ? ws[0][t] : T(0);
+        b = t < kRedThreads / 32 ? ws[1][t] : T(0);
         for (int off = 16; off > 0; off >>= 1) {
             a += __shfl_xor_sync(0xffffffffu, a, off);
             b += __shfl_xor_sync(0xffffffffu, b, off);
         }
         if (t == 0) {
-            out[0] = a;
+            out[0] = (double)a;
             if (beta_scal) {
-                beta_scal[4] = a / beta_scal[0];  // beta = rn.rn / r.r (main.py:407-409)
+                beta_scal[4] = (double)a / beta_scal[0];  // beta = rn.rn / r.r (main.py:407-409)
             } else {
-                out[1] = b;
+                out[1] = (double)b;
             }
             *counter = 0u;
         }
@@ -103,21 +110,21 @@ __device__ __forceinline__ float sqdiff4(const float4 &a, const float4 &b) {
 
 // partials[2*b + 0] = sum a*b, partials[2*b + 1] = sum c*d (or sum (a - c)^2 when DIFF).
 // n4 float4 groups (callers guarantee n % 4 == 0 and 16-byte alignment).
-template <bool DIFF>
+template <bool DIFF, class T>
 __global__ void __launch_bounds__(kRedThreads)
 dual_partials(const float4 *__restrict__ a, const float4 *__restrict__ b, const float4 *__restrict__ c,
               const float4 *__restrict__ d, size_t n4, double *__restrict__ partials, double *__restrict__ out) {
-    double s0 = 0.0, s1 = 0.0;
+    T s0 = T(0), s1 = T(0);
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n4; i += (size_t)gridDim.x * blockDim.x) {
         const float4 va = __ldg(a + i);
-        s0 += (double)dot4(va, __ldg(b + i));
+        s0 += (T)dot4(va, __ldg(b + i));
         if (DIFF) {
-            s1 += (double)sqdiff4(va, __ldg(c + i));
+            s1 += (T)sqdiff4(va, __ldg(c + i));
         } else if (c) {
-            s1 += (double)dot4(__ldg(c + i), __ldg(d + i));
+            s1 += (T)dot4(__ldg(c + i), __ldg(d + i));
         }
     }
-    finish_pairs(s0, s1, partials, out, nullptr);
+    finish_pairs<T>(s0, s1, partials, out, nullptr);
 }
 
 // Float64 inputs: partials of sum a^2 and sum (a - b)^2 with every product and
@@ -132,19 +139,20 @@ snr_partials_f64(const double *__restrict__ a, const double *__restrict__ b, siz
         s0 = __fma_rn(va, va, s0);
         s1 = __fma_rn(d, d, s1);
     }
-    finish_pairs(s0, s1, partials, out, nullptr);
+    finish_pairs<double>(s0, s1, partials, out, nullptr);
 }
 
 // Sums the kRedGrid partial pairs in a fixed order into out[0], out[1]: one
 // warp-shuffle tree per warp, then one over the warp sums.
 constexpr int kFinalizeThreads = ((kRedGrid + 31) / 32) * 32;
 
+template <class T>
 __global__ void __launch_bounds__(kFinalizeThreads)
 finalize_pairs(const double *__restrict__ partials, double *__restrict__ out) {
-    __shared__ double ws[2][kFinalizeThreads / 32];
+    __shared__ T ws[2][kFinalizeThreads / 32];
     const int t = threadIdx.x;
-    double a = t < kRedGrid ? partials[2 * t] : 0.0;
-    double b = t < kRedGrid ? partials[2 * t + 1] : 0.0;
+    T a = t < kRedGrid ? (T)partials[2 * t] : T(0);
+    T b = t < kRedGrid ? (T)partials[2 * t + 1] : T(0);
     for (int off = 16; off > 0; off >>= 1) {
         a += __shfl_xor_sync(0xffffffffu, a, off);
         b += __shfl_xor_sync(0xffffffffu, b, off);
@@ -155,15 +163,15 @@ finalize_pairs(const double *__restrict__ partials, double *__restrict__ out) {
     }
     __syncthreads();
     if (t < 32) {
-        a = t < kFinalizeThreads / 32 ? ws[0][t] : 0.0;
-        b = t < kFinalizeThreads / 32 ? ws[1][t] : 0.0;
+        a = t < kFinalizeThreads / 32 ? ws[0][t] : T(0);
+        b = t < kFinalizeThreads / 32 ? ws[1][t] : T(0);
         for (int off = 16; off > 0; off >>= 1) {
             a += __shfl_xor_sync(0xffffffffu, a, off);
             b += __shfl_xor_sync(0xffffffffu, b, off);
         }
         if (t == 0) {
-            out[0] = a;
-            out[1] = b;
+            out[0] = (double)a;
+            out[1] = (double)b;
         }
     }
 }
@@ -178,12 +186,13 @@ finalize_pairs(const double *__restrict__ partials, double *__restrict__ out) {
 // add exactly +0 to the same per-thread partial, and the sums are bit-identical
 // to the dense pass. A warp's 32 consecutive indices form one segment, so the
 // test is warp-uniform.
+template <class T>
 __global__ void __launch_bounds__(kRedThreads)
 snr_update(const float4 *__restrict__ e, float4 *__restrict__ ms, const float4 *__restrict__ q,
            const double *__restrict__ scal, size_t n4, double *__restrict__ partials,
            const unsigned char *__restrict__ seg_flags, double *__restrict__ out) {
     const float a = (float)scal[S_ALPHA];
-    double s0 = 0.0, s1 = 0.0;
+    T s0 = T(0), s1 = T(0);
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n4; i += (size_t)gridDim.x * blockDim.x) {
         if (seg_flags && seg_flags[i >> 5] == 0) continue;
         const float4 ev = __ldg(e + i), qv = __ldg(q + i);
@@ -193,10 +202,10 @@ snr_update(const float4 *__restrict__ e, float4 *__restrict__ ms, const float4 *
         mv.z = __fadd_rn(mv.z, __fmul_rn(a, qv.z));
         mv.w = __fadd_rn(mv.w, __fmul_rn(a, qv.w));
         ms[i] = mv;
-        s0 += (double)dot4(ev, ev);
-        s1 += (double)sqdiff4(ev, mv);
+        s0 += (T)dot4(ev, ev);
+        s1 += (T)sqdiff4(ev, mv);
     }
-    finish_pairs(s0, s1, partials, out, nullptr);
+    finish_pairs<T>(s0, s1, partials, out, nullptr);
 }
 
 // The vector updates evaluate the reference's float32 expressions
@@ -239,11 +248,12 @@ __global__ void cg_positivity(const float *__restrict__ x, float *__restrict__ x
 }
 
 // rn = r - alpha Ap with the per-CTA float64 partial of rn . rn (main.py:405-408).
+template <class T>
 __global__ void __launch_bounds__(kRedThreads)
 cg_residual(const float4 *__restrict__ r, const float4 *__restrict__ ap, double *__restrict__ scal,
             float4 *__restrict__ rn, size_t n4, double *__restrict__ partials) {
     const float a = (float)scal[S_ALPHA];
-    double s = 0.0;
+    T s = T(0);
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n4; i += (size_t)gridDim.x * blockDim.x) {
         const float4 rv = __ldg(r + i), av = __ldg(ap + i);
         float4 v;
@@ -252,10 +262,10 @@ cg_residual(const float4 *__restrict__ r, const float4 *__restrict__ ap, double 
         v.z = __fsub_rn(rv.z, __fmul_rn(a, av.z));
         v.w = __fsub_rn(rv.w, __fmul_rn(a, av.w));
         rn[i] = v;
-        s += (double)dot4(v, v);
+        s += (T)dot4(v, v);
     }
     // scal[S_RNRN] = rn.rn, scal[S_BETA] = rn.rn / r.r
-    finish_pairs(s, 0.0, partials, scal + S_RNRN, scal);
+    finish_pairs<T>(s, T(0), partials, scal + S_RNRN, scal);
 }
 
 // flags[s] = 1 when any element of float4 segment s (32 float4) of m is non-zero.
@@ -335,13 +345,14 @@ __global__ void mul_kernel(const float *__restrict__ a, const float *__restrict_
 }
 
 // Region sums for the standard deviation: pass 0 sums x, pass 1 sums (x - mean)^2.
+template <class T>
 __global__ void __launch_bounds__(kRedThreads)
 region_partials(const float *__restrict__ img, int pitch, int rows, int cols, int off_r, int off_c,
                 const double *__restrict__ mean_in, double *__restrict__ partials) {
     const double mean = mean_in ? mean_in[0] / ((double)rows * cols) : 0.0;
     const float mean_f = (float)mean;
     const size_t total = (size_t)rows * cols;
-    double s = 0.0;
+    T s = T(0);
     // float32 partials over runs of up to four elements per thread, float64 across runs
     float part = 0.0f;
     int run = 0;
@@ -355,15 +366,15 @@ region_partials(const float *__restrict__ img, int pitch, int rows, int cols, in
             part = __fadd_rn(part, v);
         }
         if (++run == 4) {
-            s += (double)part;
+            s += (T)part;
             part = 0.0f;
             run = 0;
         }
     }
-    s += (double)part;
-    s = block_sum(s);
+    s += (T)part;
+    s = block_sum<T>(s);
     if (threadIdx.x == 0) {
-        partials[2 * blockIdx.x] = s;
+        partials[2 * blockIdx.x] = (double)s;
         partials[2 * blockIdx.x + 1] = 0.0;
     }
 }
@@ -373,6 +384,24 @@ __global__ void std_finish(double *__restrict__ out2, long long count) {
     out2[2] = out2[0] / (double)count;
     out2[3] = sqrt(out2[1] / (double)count);
 }
+
+}  // namespace
+
+// Accumulation type of the reductions, process-wide: 64 (float64, the default)
+// or 32 (plain float32 accumulation, for the error comparison).
+std::atomic<int> g_reduce_bits{64};
+bool reduce_fp32() { return g_reduce_bits.load(std::memory_order_relaxed) == 32; }
+
+namespace {
+
+// Launches kernel template K<..., T> with T = float or double as selected.
+#define MSN_RED_LAUNCH(KERNEL, GRID, BLOCK, ST, ...)                       \
+    do {                                                                   \
+        if (reduce_fp32())                                                 \
+            KERNEL<float><<<GRID, BLOCK, 0, ST>>>(__VA_ARGS__);            \
+        else                                                               \
+            KERNEL<double><<<GRID, BLOCK, 0, ST>>>(__VA_ARGS__);           \
+    } while (0)
 
 int ew_grid(size_t n) {
     size_t g = (n + 255) / 256;
@@ -391,10 +420,15 @@ int dual_reduce(const float *a, const float *b, const float *c, const float *d, 
     if (n % 4 || !aligned16(a) || !aligned16(b) || !aligned16(c) || !aligned16(d))
         return set_error(MSN_ERR_INVALID, "reduction: length must be a multiple of 4 and pointers 16-byte aligned");
     const float4 *a4 = (const float4 *)a, *b4 = (const float4 *)b, *c4 = (const float4 *)c, *d4 = (const float4 *)d;
-    if (diff)
-        dual_partials<true><<<kRedGrid, kRedThreads, 0, st>>>(a4, b4, c4, d4, n / 4, partials, out);
+    const bool f32 = reduce_fp32();
+    if (diff && f32)
+        dual_partials<true, float><<<kRedGrid, kRedThreads, 0, st>>>(a4, b4, c4, d4, n / 4, partials, out);
+    else if (diff)
+        dual_partials<true, double><<<kRedGrid, kRedThreads, 0, st>>>(a4, b4, c4, d4, n / 4, partials, out);
+    else if (f32)
+        dual_partials<false, float><<<kRedGrid, kRedThreads, 0, st>>>(a4, b4, c4, d4, n / 4, partials, out);
     else
-        dual_partials<false><<<kRedGrid, kRedThreads, 0, st>>>(a4, b4, c4, d4, n / 4, partials, out);
+        dual_partials<false, double><<<kRedGrid, kRedThreads, 0, st>>>(a4, b4, c4, d4, n / 4, partials, out);
     return check_launch("dual_partials");
 }
 
@@ -445,7 +479,7 @@ extern "C" int msn_snr_update(const float *d_e, float *d_ms, const float *d_q, c
     MSN_TRY(check_red_ws(d_work, work_bytes, "msn_snr_update"));
     cudaStream_t st = as_stream(stream);
     double *partials = (double *)d_work;
-    snr_update<<<kRedGrid, kRedThreads, 0, st>>>((const float4 *)d_e, (float4 *)d_ms, (const float4 *)d_q, d_scal, n / 4,
+    MSN_RED_LAUNCH(snr_update, kRedGrid, kRedThreads, st, (const float4 *)d_e, (float4 *)d_ms, (const float4 *)d_q, d_scal, n / 4,
                                                   partials, nullptr, d_out2);
     return check_launch("snr_update");
 }
@@ -487,7 +521,7 @@ extern "C" int msn_snr_update_masked(const float *d_e, float *d_ms, const float 
     MSN_TRY(check_red_ws(d_work, work_bytes, "msn_snr_update_masked"));
     cudaStream_t st = as_stream(stream);
     double *partials = (double *)d_work;
-    snr_update<<<kRedGrid, kRedThreads, 0, st>>>((const float4 *)d_e, (float4 *)d_ms, (const float4 *)d_q, d_scal, n / 4,
+    MSN_RED_LAUNCH(snr_update, kRedGrid, kRedThreads, st, (const float4 *)d_e, (float4 *)d_ms, (const float4 *)d_q, d_scal, n / 4,
                                                   partials, d_flags, d_out2);
     return check_launch("snr_update");
 }
@@ -521,7 +555,7 @@ extern "C" int msn_cg_residual(const float *d_r, const float *d_ap, double *d_sc
         return set_error(MSN_ERR_INVALID, "msn_cg_residual: length must be a multiple of 4, pointers 16-byte aligned");
     cudaStream_t st = as_stream(stream);
     double *partials = (double *)d_work;
-    cg_residual<<<kRedGrid, kRedThreads, 0, st>>>((const float4 *)d_r, (const float4 *)d_ap, d_scal, (float4 *)d_rn,
+    MSN_RED_LAUNCH(cg_residual, kRedGrid, kRedThreads, st, (const float4 *)d_r, (const float4 *)d_ap, d_scal, (float4 *)d_rn,
                                                   n / 4, partials);
     return check_launch("cg_residual");
 }
@@ -574,15 +608,25 @@ extern "C" int msn_region_std(const float *d_img, int pitch, int rows, int cols,
     MSN_TRY(check_red_ws(d_work, work_bytes, "msn_region_std"));
     cudaStream_t st = as_stream(stream);
     double *partials = (double *)d_work;
-    region_partials<<<kRedGrid, kRedThreads, 0, st>>>(d_img, pitch, rows, cols, off_r, off_c, nullptr, partials);
+    MSN_RED_LAUNCH(region_partials, kRedGrid, kRedThreads, st, d_img, pitch, rows, cols, off_r, off_c, nullptr, partials);
     MSN_TRY(check_launch("region_partials"));
-    finalize_pairs<<<1, kFinalizeThreads, 0, st>>>(partials, d_out4);
+    MSN_RED_LAUNCH(finalize_pairs, 1, kFinalizeThreads, st, partials, d_out4);
     MSN_TRY(check_launch("finalize_pairs"));
-    region_partials<<<kRedGrid, kRedThreads, 0, st>>>(d_img, pitch, rows, cols, off_r, off_c, d_out4, partials);
+    MSN_RED_LAUNCH(region_partials, kRedGrid, kRedThreads, st, d_img, pitch, rows, cols, off_r, off_c, d_out4, partials);
     MSN_TRY(check_launch("region_partials"));
     // keep the first sum: write the second pair to out[1] via a temporary slot
-    finalize_pairs<<<1, kFinalizeThreads, 0, st>>>(partials, d_out4 + 1);
+    MSN_RED_LAUNCH(finalize_pairs, 1, kFinalizeThreads, st, partials, d_out4 + 1);
     MSN_TRY(check_launch("finalize_pairs"));
     std_finish<<<1, 1, 0, st>>>(d_out4, (long long)rows * cols);
     return check_launch("std_finish");
 }
+
+extern "C" int msn_set_reduction_precision(int bits) {
+    clear_error();
+    if (bits != 32 && bits != 64)
+        return set_error(MSN_ERR_INVALID, "msn_set_reduction_precision: bits must be 32 or 64, got %d", bits);
+    g_reduce_bits.store(bits);
+    return MSN_OK;
+}
+
+extern "C" int msn_reduction_precision(void) { return g_reduce_bits.load(); }

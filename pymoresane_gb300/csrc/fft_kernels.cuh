@@ -701,7 +701,7 @@ int conv_run(const float *x, int n, const float2 *spec, float *out, int linear, 
              cudaStream_t st) {
     if constexpr (M == sq::kLength) {
         // the 2048^2 linear convolution with a 4096^2 PSF: four-step kernels
-        if (linear && n == M / 2) return sq::conv_run(x, spec, out, t1, t2, st);
+        if (linear && n == M / 2 && tune_value(kKnobFourStep)) return sq::conv_run(x, spec, out, t1, t2, st);
     }
     const int off = linear ? (M - n) / 2 : 0;
     const int shift = (off + M / 2) % M;

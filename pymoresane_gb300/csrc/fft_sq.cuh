@@ -675,30 +675,39 @@ struct SqLaunch {
     int fwd_grid = 0, col_grid = 0, inv_grid = 0;
 };
 
-// Persistent grids (resident CTAs per SM x SMs), resolved once per device.
+// Persistent grids: resident CTAs per SM (the occupancy limit, or fewer when a
+// tuned value asks for it) x SMs; resolved once per device and tuning epoch.
 inline int launch_config(SqLaunch *cfg) {
     static SqLaunch cached[64];
+    static unsigned cached_epoch[64];
     int dev = 0;
     MSN_TRY(check_cuda(cudaGetDevice(&dev), "cudaGetDevice"));
-    if (dev >= 0 && dev < 64 && cached[dev].col_grid > 0) {
+    const unsigned epoch = tune_epoch();
+    if (dev >= 0 && dev < 64 && cached[dev].col_grid > 0 && cached_epoch[dev] == epoch) {
         *cfg = cached[dev];
         return MSN_OK;
     }
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (sms < 1) sms = 1;
-    auto grid_of = [&](const void *fn, int threads, size_t smem, int items) {
+    auto grid_of = [&](const void *fn, int threads, size_t smem, int items, Knob knob) {
         cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         int per_sm = 1;
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, smem);
-        const int g = (per_sm < 1 ? 1 : per_sm) * sms;
+        if (per_sm < 1) per_sm = 1;
+        const int want = tune_value(knob);
+        if (want > 0 && want < per_sm) per_sm = want;
+        const int g = per_sm * sms;
         return g < items ? g : items;
     };
     SqLaunch c;
-    c.fwd_grid = grid_of((const void *)sq_rows_fwd, R, kRowFwdSmem, PAIRS);
-    c.col_grid = grid_of((const void *)sq_cols_conv, R * TEAMS, kColSmem, (W + 1) / 2);
-    c.inv_grid = grid_of((const void *)sq_rows_inv, R, kRowInvSmem, PAIRS);
-    if (dev >= 0 && dev < 64) cached[dev] = c;
+    c.fwd_grid = grid_of((const void *)sq_rows_fwd, R, kRowFwdSmem, PAIRS, kKnobSqFwdCtas);
+    c.col_grid = grid_of((const void *)sq_cols_conv, R * TEAMS, kColSmem, (W + 1) / 2, kKnobSqColCtas);
+    c.inv_grid = grid_of((const void *)sq_rows_inv, R, kRowInvSmem, PAIRS, kKnobSqInvCtas);
+    if (dev >= 0 && dev < 64) {
+        cached[dev] = c;
+        cached_epoch[dev] = epoch;
+    }
     *cfg = c;
     return MSN_OK;
 }

@@ -135,6 +135,8 @@ struct CacheEntry {
     cudaGraphExec_t exec = nullptr;
     unsigned long long last_use = 0;
     long long prologue_kernels = 0, body_kernels = 0, branch_kernels = 0;
+    int red_bits = 64;    // reduction accumulation type the graph was captured with
+    unsigned epoch = 0;   // tuning epoch of its launch configurations
 };
 
 struct Engine {
@@ -379,8 +381,9 @@ int run_minor(Engine *e, const msn_minor_args *args, msn_minor_result *result, d
     MSN_TRY(validate_args(args));
     const msn_minor_args key = make_key(args);
     CacheEntry *ce = nullptr;
+    const int red_bits = msn_reduction_precision();
     for (auto &c : e->cache)
-        if (std::memcmp(&c.key, &key, sizeof(key)) == 0) ce = &c;
+        if (std::memcmp(&c.key, &key, sizeof(key)) == 0 && c.red_bits == red_bits && c.epoch == tune_epoch()) ce = &c;
     if (!ce) {
         if (e->cache.size() >= kMaxGraphs) {
             size_t lru = 0;
@@ -392,6 +395,8 @@ int run_minor(Engine *e, const msn_minor_args *args, msn_minor_result *result, d
         e->cache.emplace_back();
         ce = &e->cache.back();
         ce->key = key;
+        ce->red_bits = red_bits;
+        ce->epoch = tune_epoch();
         const int rc = build_graph(e, &key, ce);
         if (rc != MSN_OK) {
             destroy_entry(*ce);

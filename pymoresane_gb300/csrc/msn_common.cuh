@@ -25,6 +25,12 @@ inline int check_launch(const char *what) {
     return check_cuda(cudaGetLastError(), what);
 }
 
+// Tunable launch parameters (tune.cu): the current value of a knob, and an
+// epoch that changes whenever any knob does.
+enum Knob { kKnobFourStep = 0, kKnobSqFwdCtas, kKnobSqColCtas, kKnobSqInvCtas, kKnobIuwtThreads, kKnobCount };
+int tune_value(Knob k);
+unsigned tune_epoch();
+
 inline cudaStream_t as_stream(void *s) { return reinterpret_cast<cudaStream_t>(s); }
 
 inline bool aligned16(const void *p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }

@@ -25,6 +25,7 @@ from . import _native
 from .beam_fit import beam_fit
 from . import device as dev
 from . import fits
+from . import tune
 
 logger = logging.getLogger(__name__)
 
@@ -149,6 +150,7 @@ class Deconvolver:
 
     def __init__(self, psf, mask=None, dirty_shape=None, workspace=None):
         dev.require_cuda()
+        tune.ensure_applied()  # this device's cached autotuner choices, once per process
         _native.load()
         self.device = torch.device("cuda", torch.cuda.current_device())
         self.psf = dev.as_f32_cuda(psf, device=self.device)

@@ -1,0 +1,185 @@
+"""Autotuner for libmsn's launch parameters.
+
+The library reads a few tunable launch parameters at every launch (declared
+with msn_tune_set in include/msn.h): which kernels run the 2048^2 linear
+convolution with a 4096^2 PSF (the four-step kernels or the Stockham ones),
+how many CTAs of each four-step kernel share an SM, and how many threads a CTA
+of the a trous passes has. None of them changes a result; they only change the
+speed, and the best values depend on the device.
+
+``autotune()`` times the candidates of each parameter on the real operation
+(CUDA events on the current stream, the median of several runs after a
+warm-up), keeps the fastest, sets it in the library and stores the choice in a
+JSON cache keyed by the device (name, SM count, compute capability).
+``ensure_applied()`` loads the cache once per process and sets the cached
+values; the deconvolution driver calls it, so a tuned device keeps its choices
+across processes. The cache lives in ``$PYMORESANE_GB300_TUNE_CACHE`` or
+``~/.cache/pymoresane_gb300/tune.json``.
+
+Parameters are tuned one after another (coordinate descent from the current
+values): first the convolution kernels, then each four-step CTA count, then
+the a trous CTA size.
+"""
+import ctypes
+import json
+import os
+import statistics
+import threading
+
+from . import _native
+
+CACHE_ENV = "PYMORESANE_GB300_TUNE_CACHE"
+KNOBS = ("fft_four_step", "fft_sq_fwd_ctas", "fft_sq_col_ctas", "fft_sq_inv_ctas", "iuwt_threads")
+CANDIDATES = {
+    "fft_four_step": (1, 0),
+    "fft_sq_fwd_ctas": (0, 2, 3),
+    "fft_sq_col_ctas": (0, 2),
+    "fft_sq_inv_ctas": (0, 2),
+    "iuwt_threads": (256, 128, 64),
+}
+_applied = False
+_lock = threading.Lock()
+
+
+def cache_path():
+    return os.environ.get(CACHE_ENV) or os.path.join(os.path.expanduser("~"), ".cache", "pymoresane_gb300",
+                                                     "tune.json")
+
+
+def load_cache(path=None):
+    path = path or cache_path()
+    try:
+        with open(path) as fh:
+            data = json.load(fh)
+        return data if isinstance(data, dict) else {}
+    except (OSError, ValueError):
+        return {}
+
+
+def save_cache(data, path=None):
+    path = path or cache_path()
+    os.makedirs(os.path.dirname(path) or ".", exist_ok=True)
+    tmp = path + ".tmp"
+    with open(tmp, "w") as fh:
+        json.dump(data, fh, indent=1, sort_keys=True)
+    os.replace(tmp, path)
+    return path
+
+
+def device_key():
+    import torch
+    p = torch.cuda.get_device_properties(torch.cuda.current_device())
+    return f"{p.name}|sm{p.multi_processor_count}|cc{p.major}.{p.minor}"
+
+
+def get(name):
+    v = ctypes.c_int()
+    _native.call("msn_tune_get", name.encode(), ctypes.byref(v))
+    return v.value
+
+
+def current():
+    return {k: get(k) for k in KNOBS}
+
+
+def set_values(values):
+    for k, v in values.items():
+        if k in KNOBS:
+            _native.call("msn_tune_set", k.encode(), int(v))
+
+
+def reset():
+    _native.call("msn_tune_reset")
+
+
+def choose(name, candidates, measure):
+    """Sets each candidate value of ``name``, calls ``measure()`` (seconds) and keeps the fastest.
+
+    Returns (best value, {value: seconds}); the library is left at the best value.
+    """
+    times = {}
+    for v in candidates:
+        set_values({name: v})
+        times[v] = measure()
+    best = min(times, key=times.get)
+    set_values({name: best})
+    return best, times
+
+
+def _timer(fn, reps, warmup=2):
+    import torch
+    stream = torch.cuda.current_stream()
+
+    def measure():
+        for _ in range(warmup):
+            fn()
+        vals = []
+        for _ in range(reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+            e1.synchronize()
+            vals.append(e0.elapsed_time(e1) * 1e-3)
+        return statistics.median(vals)
+    return measure
+
+
+def autotune(n=2048, reps=10, path=None, save=True):
+    """Tunes every parameter on an n x n problem (convolution with a 2n x 2n PSF spectrum,
+    decomposition + recomposition with log2(n) - 4 scales) and caches the result.
+
+    Returns {"device": key, "values": {...}, "times_s": {...}}.
+    """
+    import numpy as np
+    import torch
+
+    from . import device as dev
+    from . import synthetic
+    rng = np.random.default_rng(0)
+    x = torch.from_numpy(rng.standard_normal((n, n)).astype(np.float32)).cuda()
+    psf = synthetic.make_psf(2 * n, 2000, rng)
+    spec = dev.psf_spectrum(psf)
+    out = torch.empty_like(x)
+    fwork = dev.fft_workspace(n, 2 * n, x.device)
+    scales = max(2, int(np.log2(n)) - 4)
+    w = torch.empty((scales, n, n), dtype=torch.float32, device=x.device)
+    c = torch.empty_like(x)
+    rec = torch.empty_like(x)
+    iwork = dev.iuwt_workspace(n, n, x.device)
+
+    def conv():
+        dev.fft_convolve(x, spec, True, out=out, work=fwork)
+
+    def iuwt():
+        dev.iuwt_decompose(x, scales, 0, store_smoothed=True, out=w, smoothed_out=c, work=iwork)
+        dev.iuwt_recompose(w, 0, smoothed=c, out=rec, work=iwork)
+
+    times = {}
+    for name in KNOBS:
+        if name.startswith("fft_sq_") and get("fft_four_step") == 0:
+            continue
+        op = iuwt if name == "iuwt_threads" else conv
+        best, t = choose(name, CANDIDATES[name], _timer(op, reps))
+        times[name] = {str(k): v for k, v in t.items()}
+    torch.cuda.synchronize()
+    result = {"device": device_key(), "n": n, "values": current(), "times_s": times}
+    if save:
+        data = load_cache(path)
+        data[device_key()] = result
+        save_cache(data, path)
+    return result
+
+
+def ensure_applied(path=None):
+    """Sets the cached values for this device once per process; returns them (or None)."""
+    global _applied
+    with _lock:
+        if _applied:
+            return None
+        _applied = True
+        entry = load_cache(path).get(device_key())
+        if not entry:
+            return None
+        set_values(entry.get("values", {}))
+        return entry.get("values")

@@ -231,11 +231,35 @@ def gen_baseline_2048_full(ref):
     _gen_2048(ref, "baseline_2048_full", BASELINE_2048_RUN["major_loop_miter"])
 
 
+def gen_oracle_f64_2048_m3(ref):
+    """The float64 oracle (oracle/moresane.py, precision='f64': the reference's float32
+    casts removed) on the 2048^2 problem, three major iterations: the yardstick of
+    the float32 versus float64-reduction error statement. Does not use `ref`."""
+    from oracle.moresane import MoresaneOracle
+    from pymoresane_gb300 import synthetic
+    dirty, psf, _ = synthetic.make_problem(synthetic.problem_2048(0))
+    kw = dict(BASELINE_2048_RUN, major_loop_miter=3)
+    o = MoresaneOracle(dirty, psf, precision="f64")
+    t0 = time.perf_counter()
+    o.moresane(subregion=dirty.shape[0], **kw)
+    dt = time.perf_counter() - t0
+    flat = o.model.ravel()
+    idx = np.flatnonzero(flat).astype(np.int64)
+    n = dirty.shape[0]
+    c = slice(n // 2 - 128, n // 2 + 128)
+    recs = np.array([[r["max_scale"], r["scale_adjust"], r["minor"], int(r["reverted"])] for r in o.log], np.int64)
+    print("oracle_f64_2048_m3 majors", len(o.log), "seconds", round(dt, 1), "nnz", idx.size)
+    save("oracle_f64_2048_m3", dirty_sha=digest(dirty), psf_sha=digest(psf), model_idx=idx, model_val=flat[idx],
+         model_shape=np.array(o.model.shape), residual_std=np.array(np.std(o.residual)),
+         residual_rms=np.array(np.sqrt(np.mean(np.square(o.residual)))), residual_centre=o.residual[c, c],
+         records=recs, seconds=np.array(dt))
+
+
 GENERATORS = {"restore": gen_restore, "iuwt": gen_iuwt, "conv": gen_conv, "toolbox": gen_toolbox, "moresane": gen_moresane,
               "tart": gen_tart, "baseline_512": gen_baseline_512, "baseline_2048_m3": gen_baseline_2048_m3,
-              "baseline_2048_full": gen_baseline_2048_full}
+              "baseline_2048_full": gen_baseline_2048_full, "oracle_f64_2048_m3": gen_oracle_f64_2048_m3}
 # slow: run only when named with --only
-SLOW = {"baseline_512", "baseline_2048_m3", "baseline_2048_full"}
+SLOW = {"baseline_512", "baseline_2048_m3", "baseline_2048_full", "oracle_f64_2048_m3"}
 
 
 def main():

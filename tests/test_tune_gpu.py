@@ -1,0 +1,35 @@
+"""The autotuner on the GPU: it picks values, and no value changes a result."""
+import numpy as np
+import pytest
+import torch
+
+from pymoresane_gb300 import device as dev
+from pymoresane_gb300 import synthetic, tune
+
+pytestmark = pytest.mark.gpu
+
+
+def test_autotune_choices_do_not_change_results(cuda, tmp_path):
+    rng = np.random.default_rng(11)
+    x = torch.from_numpy(rng.standard_normal((2048, 2048)).astype(np.float32)).cuda()
+    spec = dev.psf_spectrum(synthetic.make_psf(4096, 3000, rng))
+    tune.reset()
+    try:
+        ref = dev.fft_convolve(x, spec).clone()
+        w_ref = dev.iuwt_decompose(x, 6, 0)[0].clone()
+        res = tune.autotune(n=2048, reps=3, path=str(tmp_path / "tune.json"))
+        assert set(res["values"]) == set(tune.KNOBS)
+        assert tune.load_cache(str(tmp_path / "tune.json"))[tune.device_key()]["values"] == res["values"]
+        # every candidate of every knob gives the same convolution (within the FFT tolerance) and the
+        # same wavelet coefficients (bit for bit)
+        for four_step in (0, 1):
+            for ctas in (0, 2):
+                tune.set_values({"fft_four_step": four_step, "fft_sq_col_ctas": ctas, "fft_sq_fwd_ctas": ctas,
+                                 "fft_sq_inv_ctas": ctas})
+                got = dev.fft_convolve(x, spec)
+                assert torch.max(torch.abs(got - ref)).item() <= 1e-5 * torch.max(torch.abs(ref)).item()
+        for threads in (64, 128, 256):
+            tune.set_values({"iuwt_threads": threads})
+            assert torch.equal(dev.iuwt_decompose(x, 6, 0)[0], w_ref)
+    finally:
+        tune.reset()
