@@ -362,7 +362,7 @@ def mix_job(n, seed):
     """The 512^2 problem's recipe scaled by area to side n (PSF 2n, uv count and sources ~ n^2), S = log2(n) - 3."""
     from pymoresane_gb300 import synthetic
     from pymoresane_gb300.batch import Job
-    dirty, psf, _ = synthetic.make_problem(synthetic.scaled(n, seed=seed))
+    dirty, psf, _ = synthetic.make_problem(synthetic.scaled(n, seed=seed), fast=True)
     return Job(dirty, psf, kwargs=dict(MIX_KW, scale_count=int(np.log2(n)) - 3), tag=(n, seed))
 
 
@@ -511,6 +511,7 @@ def main():
     ap.add_argument("--served-jobs", type=int, default=8, help="deconv: jobs of the served 2048^2 measurement (0: skip)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-tune", action="store_true", help="skip the autotuner (use the current launch parameters)")
+    ap.add_argument("--no-mix", action="store_true", help="deconv: skip the batched and served mixed-size workloads")
     ap.add_argument("--driver", default="native", choices=["native", "host"],
                     help="deconv: native = minor/major loops in libmsn (graphs); host = step by step (for ncu)")
     args = ap.parse_args()
@@ -664,6 +665,28 @@ def main():
     served = None
     if args.served_jobs > 0 and args.driver == "native":
         served = run_served_2048(args, res["dirty"], res["psf"], res["model"])
+    mix = {}
+    if not args.no_mix and args.driver == "native":
+        # the batched (64 mixed-size images) and served (Poisson arrivals) workloads, in the same line
+        for name, fn in (("batch", run_batch), ("serve", run_serve)):
+            r = fn(args, rank)
+            n_img = r["images"] if name == "batch" else r["requests"]
+            mixed_s = r["batch_s"] if name == "batch" else r["wall_s"]
+            mixed_s, plain_s = replicas.reduce_max([mixed_s, r["plain_s"]], dist, "cuda")
+            mix[name] = {
+                "value": replicas.whole_job_rate(n_img, world, mixed_s), "unit": "images/s",
+                "plain": replicas.whole_job_rate(n_img, world, plain_s), "speedup_vs_plain": plain_s / mixed_s,
+                "latency_ms": {"p50": percentile(r["lat"], 50), "p99": percentile(r["lat"], 99)},
+                "sizes": r["sizes"], "distinct_problems_per_size": args.distinct, "workers": args.workers,
+                "same_result_alone_and_in_mix": r["same"]}
+            if name == "batch":
+                mix[name]["images"] = n_img
+            else:
+                mix[name].update(requests=n_img, rate_per_s=args.rate, specified_requests=2000,
+                                 arrival_span_s=r["arrival_span_s"],
+                                 plain_latency_ms={"p50": percentile(r["seq_lat"], 50),
+                                                   "p99": percentile(r["seq_lat"], 99),
+                                                   "mode": "same arrivals served one at a time"})
     ms_per_step = res["ms"] / args.steps
     value = world * args.steps / (res["ms"] * 1e-3)
     iuwt = measure_iuwt(5, 3, seed=rank)
@@ -697,7 +720,8 @@ def main():
                     "d2h_bytes_per_step": 8 * n * n, "steps": res["e2e_steps"],
                     "api": "pymoresane_gb300.main.DataImage(dirty, psf).moresane(...) with host numpy arrays"},
             "gpu_launches": res["launches"], "clocks": res["clocks"], "cpu_baseline": cpu,
-            "served": served, "autotuned": tuned,
+            "served": served, "batched_64_mixed": mix.get("batch"), "served_poisson": mix.get("serve"),
+            "autotuned": tuned,
         }))
     if dist:
         dist.destroy_process_group()

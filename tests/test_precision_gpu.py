@@ -90,3 +90,33 @@ def test_reduction_precision_setting(cuda):
     with pytest.raises(ValueError):
         _native.call("msn_set_reduction_precision", 16)
     assert _native.query("msn_reduction_precision") == 64
+
+
+def test_float32_reductions_on_a_long_run(cuda):
+    # the 512^2 problem run to completion (62 major iterations in the reference's own run,
+    # tests/golden/baseline_512.npz): float32 accumulation against the float64 default, both
+    # measured against the reference's result; stated, not bounded, for float32
+    path = os.path.join(GOLDEN, "baseline_512.npz")
+    if not os.path.exists(path):
+        pytest.skip("baseline_512.npz not generated")
+    g = np.load(path)
+    dirty, psf, _ = synthetic.make_problem(synthetic.problem_512(0))
+    ref = np.zeros(int(np.prod(g["model_shape"])), np.float32)
+    ref[g["model_idx"]] = g["model_val"]
+    ref = ref.reshape(tuple(g["model_shape"]))
+    peak = float(np.max(np.abs(ref)))
+    ref_majors = int(g["major"])
+    out = {}
+    for bits in (64, 32):
+        _native.call("msn_set_reduction_precision", bits)
+        try:
+            img = DataImage(dirty, psf, None, 1.0, 1.0)
+            img.moresane(subregion=dirty.shape[0], **mg.BASELINE_RUN)
+        finally:
+            _native.call("msn_set_reduction_precision", 64)
+        out[bits] = (float(np.max(np.abs(img.model - ref))) / peak, len(img.log),
+                     sum(r["minor"] for r in img.log))
+    print(f"\n512^2 run to completion against the reference ({ref_majors} major iterations): "
+          + "; ".join(f"{'float64' if b == 64 else 'float32'} reductions: model {e:.2e} of peak, {mj} major / "
+                      f"{mn} minor iterations" for b, (e, mj, mn) in out.items()))
+    assert out[64][0] <= 2e-4 and abs(out[64][1] - ref_majors) <= 1
