@@ -52,7 +52,7 @@ unsigned long long msn_launch_count(int reset);
 
 /* Bytes of scratch needed by msn_iuwt_decompose / msn_iuwt_recompose for an
  * ny x nx image (two planes). */
-size_t msn_iuwt_workspace_bytes(int ny, int nx);
+size_t msn_iuwt_workspace_bytes(int ny, int nx);  /* four planes of scratch */
 
 /* Replaces iuwt_decomposition(in1, scale_count, scale_adjust, mode='gpu',
  * store_smoothed=...) -- pymoresane/iuwt.py:17 -> gpu_iuwt_decomposition
@@ -105,6 +105,16 @@ int msn_recompose_row_activity(const unsigned char *d_row_flags, int planes, int
  * stack that is zero outside the flagged rows (up to the sign of zeros). */
 int msn_iuwt_recompose_rows(const float *d_detail, int planes, const unsigned char *d_act, float *d_out, int ny,
                             int nx, int scale_adjust, void *d_work, size_t work_bytes, void *stream);
+
+/* msn_iuwt_recompose_rows without the zero writes: rows that d_act marks
+ * inactive are neither computed nor written. The caller guarantees that they
+ * already hold zeros in d_out and in planes 2 and 3 of the workspace (clear
+ * both once, e.g. with cudaMemsetAsync, before the calls that share one
+ * activity map; transforms sharing the workspace only use its planes 0 and 1).
+ * No counterpart in the reference (the minor loop's A p, main.py:375-384,
+ * applied to a detail stack that is zero outside the mask rows). */
+int msn_iuwt_recompose_active_rows(const float *d_detail, int planes, const unsigned char *d_act, float *d_out,
+                                   int ny, int nx, int scale_adjust, void *d_work, size_t work_bytes, void *stream);
 
 /* Same result as msn_iuwt_decompose, but the two scratch planes come from a
  * fixed device array inside libmsn.so instead of a caller workspace, so the

@@ -29,6 +29,8 @@ SIGNATURES = {
     "msn_recompose_row_activity": (c_int, [c_void_p, c_int, c_int, c_int, c_void_p, c_void_p]),
     "msn_iuwt_recompose_rows": (c_int, [c_void_p, c_int, c_void_p, c_void_p, c_int, c_int, c_int, c_void_p, c_size_t,
                                         c_void_p]),
+    "msn_iuwt_recompose_active_rows": (c_int, [c_void_p, c_int, c_void_p, c_void_p, c_int, c_int, c_int, c_void_p,
+                                               c_size_t, c_void_p]),
     "msn_iuwt_recompose": (c_int, [c_void_p, c_int, c_void_p, c_void_p, c_int, c_int, c_int, c_void_p, c_size_t,
                                    c_void_p]),
     "msn_iuwt_decompose_static": (c_int, [c_void_p, c_void_p, c_void_p, c_int, c_int, c_int, c_int, c_void_p]),

@@ -87,13 +87,14 @@ template <int EPI>
 __global__ void __launch_bounds__(kThreads)
 atrous_band(const float *__restrict__ in, float *__restrict__ out, const float *__restrict__ aux,
             const float *__restrict__ mask, int ny, int nx, int d, int band_rows,
-            const unsigned char *__restrict__ row_flags) {
+            const unsigned char *__restrict__ row_flags, int skip_inactive) {
     extern __shared__ float4 smem4[];
     // masked detail with row flags: rows whose mask row is empty are left as they are (zero)
     if (EPI == kDetailMask && row_flags && band_rows == 1 && !row_flags[blockIdx.x]) return;
     // recomposition with row activity: an inactive output row is exactly zero (all its
     // taps and its detail row are zero), so it is written as zeros without reading anything
     if ((EPI == kAdd || EPI == kStore) && row_flags && band_rows == 1 && !row_flags[blockIdx.x]) {
+        if (skip_inactive) return;  // the caller keeps inactive rows at zero
         float4 *o4 = reinterpret_cast<float4 *>(out) + (size_t)blockIdx.x * (nx >> 2);
         for (int j = threadIdx.x; j < (nx >> 2); j += blockDim.x) o4[j] = make_float4(0.f, 0.f, 0.f, 0.f);
         return;
@@ -258,6 +259,22 @@ __global__ void zero_plus(const float4 *__restrict__ w, float4 *__restrict__ out
     }
 }
 
+// rec = 0 + w on the rows act marks active (one row per CTA); inactive rows are
+// not touched (the caller keeps them at zero).
+__global__ void zero_plus_rows(const float4 *__restrict__ w, float4 *__restrict__ out, int nx4,
+                               const unsigned char *__restrict__ act) {
+    if (!act[blockIdx.x]) return;
+    const size_t base = (size_t)blockIdx.x * nx4;
+    for (int j = threadIdx.x; j < nx4; j += blockDim.x) {
+        float4 v = __ldg(w + base + j);
+        v.x = __fadd_rn(0.0f, v.x);
+        v.y = __fadd_rn(0.0f, v.y);
+        v.z = __fadd_rn(0.0f, v.z);
+        v.w = __fadd_rn(0.0f, v.w);
+        out[base + j] = v;
+    }
+}
+
 // One row per CTA. Measured on GB300 (one smoothing pass, d = 1 .. 256):
 // 2048^2 10.3-14.4 us and 4096^2 33.9-45.1 us with one row, against 12.4-16.4
 // and 43.0-63.5 us with three; a plain float4 copy of the same plane takes
@@ -267,7 +284,7 @@ int band_rows_for(int, int) { return 1; }
 
 template <int EPI>
 int launch_band(const float *in, float *out, const float *aux, int ny, int nx, int d, cudaStream_t st,
-                const float *mask = nullptr, const unsigned char *row_flags = nullptr) {
+                const float *mask = nullptr, const unsigned char *row_flags = nullptr, int skip_inactive = 0) {
     static std::once_flag once;
     std::call_once(once, [] {
         cudaFuncSetAttribute(atrous_band<EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxSmem);
@@ -278,7 +295,7 @@ int launch_band(const float *in, float *out, const float *aux, int ny, int nx, i
     const int work4 = band * (nx >> 2);
     const int cta = tune_value(kKnobIuwtThreads);  // 64, 128 or 256 (<= kThreads)
     const int threads = work4 >= cta ? cta : ((work4 + 31) / 32) * 32;
-    atrous_band<EPI><<<grid, threads, smem, st>>>(in, out, aux, mask, ny, nx, d, band, row_flags);
+    atrous_band<EPI><<<grid, threads, smem, st>>>(in, out, aux, mask, ny, nx, d, band, row_flags, skip_inactive);
     return check_launch("atrous_band");
 }
 
@@ -337,8 +354,8 @@ int iuwt_smooth_detail(const float *in, const float *c0, float *w, int ny, int n
     return launch_band<kDetail>(in, w, c0, ny, nx, 1 << scale, st);
 }
 int iuwt_smooth_add(const float *in, const float *w, float *out, int ny, int nx, int scale, cudaStream_t st,
-                    const unsigned char *row_act = nullptr) {
-    return launch_band<kAdd>(in, out, w, ny, nx, 1 << scale, st, nullptr, row_act);
+                    const unsigned char *row_act = nullptr, int skip_inactive = 0) {
+    return launch_band<kAdd>(in, out, w, ny, nx, 1 << scale, st, nullptr, row_act, skip_inactive);
 }
 int iuwt_smooth_detail_mask(const float *in, const float *c0, const float *mask, float *w, int ny, int nx, int scale,
                             cudaStream_t st, const unsigned char *row_flags = nullptr) {
@@ -435,9 +452,12 @@ int iuwt_decompose_impl(const float *d_in, float *d_detail, float *d_smoothed, i
 // d_act (may be null): [max_scale][ny] bytes, row r of the level of scale s is
 // active when d_act[s * ny + r] != 0 (msn_recompose_row_activity); inactive rows
 // are written as zeros without being computed.
+// skip_inactive (with d_act, no smoothed plane): inactive rows are neither
+// computed nor written; the caller guarantees they already hold zeros in d_out
+// and in p0 / p1 (msn_iuwt_recompose_active_rows).
 int iuwt_recompose_impl(const float *d_detail, int planes, const float *d_smoothed, float *d_out, int ny, int nx,
                         int scale_adjust, float *p0, float *p1, cudaStream_t st,
-                        const unsigned char *d_act = nullptr) {
+                        const unsigned char *d_act = nullptr, int skip_inactive = 0) {
     const size_t plane = (size_t)ny * nx;
     float *bufs[2] = {p0, p1};
     const int max_scale = planes + scale_adjust;
@@ -452,10 +472,15 @@ int iuwt_recompose_impl(const float *d_detail, int planes, const float *d_smooth
         int nb;
         float *dst = dst_for(nb);
         const float *w = d_detail + (size_t)(s - scale_adjust) * plane;
-        if (cur == nullptr) {
+        if (cur == nullptr && skip_inactive) {
+            zero_plus_rows<<<ny, 128, 0, st>>>(reinterpret_cast<const float4 *>(w), reinterpret_cast<float4 *>(dst),
+                                               nx / 4, d_act + (size_t)s * ny);
+            MSN_TRY(check_launch("zero_plus_rows"));
+        } else if (cur == nullptr) {
             MSN_TRY(launch_zero_plus(w, dst, plane, st));
         } else {
-            MSN_TRY(iuwt_smooth_add(cur, w, dst, ny, nx, s, st, d_act ? d_act + (size_t)s * ny : nullptr));
+            MSN_TRY(iuwt_smooth_add(cur, w, dst, ny, nx, s, st, d_act ? d_act + (size_t)s * ny : nullptr,
+                                    skip_inactive));
         }
         cur = dst;
         cur_buf = (dst == d_out) ? -1 : nb;
@@ -466,7 +491,8 @@ int iuwt_recompose_impl(const float *d_detail, int planes, const float *d_smooth
         if (cur == nullptr) {
             MSN_TRY(check_cuda(cudaMemsetAsync(dst, 0, plane * sizeof(float), st), "zero plane"));
         } else if (d_act) {
-            MSN_TRY(launch_band<kStore>(cur, dst, nullptr, ny, nx, 1 << s, st, nullptr, d_act + (size_t)s * ny));
+            MSN_TRY(launch_band<kStore>(cur, dst, nullptr, ny, nx, 1 << s, st, nullptr, d_act + (size_t)s * ny,
+                                        skip_inactive));
         } else {
             MSN_TRY(iuwt_smooth(cur, dst, ny, nx, s, st));
         }
@@ -500,7 +526,9 @@ using namespace msn;
 
 extern "C" size_t msn_iuwt_workspace_bytes(int ny, int nx) {
     if (ny <= 0 || nx <= 0) return 0;
-    return 2 * plane_stride_bytes(ny, nx);
+    // planes 0, 1: every transform's scratch; planes 2, 3: the recomposition of
+    // msn_iuwt_recompose_active_rows, whose inactive rows the caller keeps at zero
+    return 4 * plane_stride_bytes(ny, nx);
 }
 
 extern "C" int msn_iuwt_decompose(const float *d_in, float *d_detail, float *d_smoothed, int ny, int nx,
@@ -586,6 +614,26 @@ extern "C" int msn_iuwt_recompose_rows(const float *d_detail, int planes, const 
     MSN_TRY(split_workspace(d_work, work_bytes, ny, nx, &p0, &p1, fn));
     return iuwt_recompose_impl(d_detail, planes, nullptr, d_out, ny, nx, scale_adjust, p0, p1, as_stream(stream),
                                d_act);
+}
+
+extern "C" int msn_iuwt_recompose_active_rows(const float *d_detail, int planes, const unsigned char *d_act,
+                                              float *d_out, int ny, int nx, int scale_adjust, void *d_work,
+                                              size_t work_bytes, void *stream) {
+    clear_error();
+    static const char *fn = "msn_iuwt_recompose_active_rows";
+    MSN_TRY(validate_image(ny, nx, fn));
+    if (planes < 1 || scale_adjust < 0) return set_error(MSN_ERR_INVALID, "%s: planes=%d scale_adjust=%d", fn, planes,
+                                                         scale_adjust);
+    MSN_TRY(validate_scales(ny, nx, planes + scale_adjust, fn));
+    if (!d_detail || !d_act || !d_out) return set_error(MSN_ERR_INVALID, "%s: null pointer", fn);
+    if (!aligned16(d_detail) || !aligned16(d_out)) return set_error(MSN_ERR_INVALID, "%s: pointers not 16-byte aligned", fn);
+    float *p0, *p1;
+    MSN_TRY(split_workspace(d_work, work_bytes, ny, nx, &p0, &p1, fn));
+    const size_t stride = plane_stride_bytes(ny, nx);
+    float *q0 = reinterpret_cast<float *>(reinterpret_cast<char *>(d_work) + 2 * stride);
+    float *q1 = reinterpret_cast<float *>(reinterpret_cast<char *>(d_work) + 3 * stride);
+    return iuwt_recompose_impl(d_detail, planes, nullptr, d_out, ny, nx, scale_adjust, q0, q1, as_stream(stream), d_act,
+                               1);
 }
 
 extern "C" int msn_iuwt_recompose(const float *d_detail, int planes, const float *d_smoothed, float *d_out, int ny,

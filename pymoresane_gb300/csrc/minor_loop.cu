@@ -198,9 +198,10 @@ int apply_a(const msn_minor_args *a, const float *in, float *out, cudaStream_t s
     // rows whose mask row is empty stay zero (cleared in the prologue)
     MSN_TRY(msn_iuwt_decompose_masked_rows(a->tmp, a->emask, a->row_flags, a->planes, a->n, a->n, a->max_scale,
                                            a->scale_adjust, a->iuwt_work, a->iuwt_work_bytes, st));
-    // rows outside the recomposition's support (fixed for the minor loop) are written as zeros
-    return msn_iuwt_recompose_rows(a->planes, planes, a->rec_rows, out, a->n, a->n, a->scale_adjust, a->iuwt_work,
-                                   a->iuwt_work_bytes, st);
+    // rows outside the recomposition's support (fixed for the minor loop) are never touched: the
+    // prologue cleared them in A p and in the recomposition planes of the workspace
+    return msn_iuwt_recompose_active_rows(a->planes, planes, a->rec_rows, out, a->n, a->n, a->scale_adjust,
+                                          a->iuwt_work, a->iuwt_work_bytes, st);
 }
 
 // Adds a conditional node after the current capture dependencies of st and
@@ -264,6 +265,9 @@ int build_graph(Engine *e, const msn_minor_args *a, CacheEntry *ce) {
         MSN_TRY(msn_row_flags(a->emask, (size_t)planes * a->n, a->n, a->row_flags, st));
         MSN_TRY(msn_recompose_row_activity(a->row_flags, planes, a->n, a->scale_adjust, a->rec_rows, st));
         MSN_TRY(check_cuda(cudaMemsetAsync(a->planes, 0, (size_t)planes * nvec * sizeof(float), st), "zero Q"));
+        // A p and the recomposition planes: rows outside the recomposition's support stay zero
+        MSN_TRY(check_cuda(cudaMemsetAsync(a->ap, 0, nvec * sizeof(float), st), "zero Ap"));
+        MSN_TRY(check_cuda(cudaMemsetAsync(a->iuwt_work, 0, a->iuwt_work_bytes, st), "zero IUWT workspace"));
         minor_init<<<1, 1, 0, st>>>(state, a->minor_loop_miter);
         MSN_TRY(check_launch("minor_init"));
         return add_conditional(st, while_h, cudaGraphCondTypeWhile, &body);

@@ -46,7 +46,7 @@ def test_signature_table_matches_header():
 def test_host_queries(lib):
     _native.load()
     assert _native.query("msn_version") >= 100
-    assert _native.query("msn_iuwt_workspace_bytes", 64, 64) == 2 * 64 * 64 * 4
+    assert _native.query("msn_iuwt_workspace_bytes", 64, 64) == 4 * 64 * 64 * 4
     assert _native.query("msn_iuwt_workspace_bytes", 0, 64) == 0
     assert _native.query("msn_last_error") == b""
 

@@ -198,3 +198,12 @@ def test_recompose_rows_matches_dense(cuda, n, planes, adj, blobs):
     # the activity covers every non-zero row of the result
     rows = (d != 0).any(axis=1)
     assert not np.any(rows & ~act.cpu().numpy()[:n].astype(bool))
+    # the variant that never touches inactive rows: cleared output and recomposition planes, two calls
+    # in a row with one activity map (as the minor loop calls it), and a second stack on the same map
+    out2 = torch.zeros((n, n), device="cuda")
+    work.zero_()
+    for stack in (wt, wt * 0.5):
+        _native.call("msn_iuwt_recompose_active_rows", stack.data_ptr(), planes, act.data_ptr(), out2.data_ptr(), n,
+                     n, adj, work.data_ptr(), work.numel(), st)
+        work[:2 * ((n * n * 4 + 255) // 256 * 256)].fill_(0x7f)   # planes 0 and 1 are free scratch
+        assert np.array_equal(out2.cpu().numpy(), dev.iuwt_recompose(stack, adj).cpu().numpy())
