@@ -328,6 +328,13 @@ int msn_cg_positivity(const float *d_x, float *d_xn, float *d_p, const double *d
 int msn_cg_residual(const float *d_r, const float *d_ap, double *d_scal, float *d_rn, size_t n, void *d_work,
                     size_t work_bytes, void *stream);
 
+/* msn_cg_alpha_x (without the negative count) and msn_cg_residual in one
+ * pass, for the minor loop without positivity (main.py:386-390,405-409):
+ * xn = x + alpha p, rn = r - alpha Ap, rn.rn and beta; bit-identical to the
+ * two calls. */
+int msn_cg_step(const float *d_x, const float *d_p, const float *d_r, const float *d_ap, double *d_scal, float *d_xn,
+                float *d_rn, size_t n, void *d_work, size_t work_bytes, void *stream);
+
 /* p = rn + beta p (pymoresane/main.py:411). */
 int msn_cg_direction(const float *d_rn, float *d_p, const double *d_scal, size_t n, void *stream);
 

@@ -74,6 +74,8 @@ SIGNATURES = {
     "msn_cg_alpha_x": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_size_t, c_void_p, c_void_p]),
     "msn_cg_positivity": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_size_t, c_void_p]),
     "msn_cg_residual": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_size_t, c_void_p, c_size_t, c_void_p]),
+    "msn_cg_step": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_size_t, c_void_p,
+                            c_size_t, c_void_p]),
     "msn_cg_direction": (c_int, [c_void_p, c_void_p, c_void_p, c_size_t, c_void_p]),
     "msn_model_update": (c_int, [c_void_p, c_int, c_void_p, c_int, c_int, c_int, c_float, c_int, c_void_p]),
     "msn_sub": (c_int, [c_void_p, c_void_p, c_void_p, c_size_t, c_void_p]),

@@ -268,6 +268,37 @@ cg_residual(const float4 *__restrict__ r, const float4 *__restrict__ ap, double 
     finish_pairs<T>(s, T(0), partials, scal + S_RNRN, scal);
 }
 
+// One pass of the step without positivity: xn = x + alpha p and rn = r - alpha Ap
+// with the float64 partials of rn . rn (then rn.rn and beta), the arithmetic of
+// cg_alpha_x followed by cg_residual. The reduction uses cg_residual's grid and
+// order, so rn.rn and beta are bit-identical to the two-kernel sequence.
+template <class T>
+__global__ void __launch_bounds__(kRedThreads)
+cg_step(const float4 *__restrict__ x, const float4 *__restrict__ p, const float4 *__restrict__ r,
+        const float4 *__restrict__ ap, double *__restrict__ scal, float4 *__restrict__ xn, float4 *__restrict__ rn,
+        size_t n4, double *__restrict__ partials) {
+    const double alpha = scal[S_RR] / scal[S_PAP];
+    if (blockIdx.x == 0 && threadIdx.x == 0) scal[S_ALPHA] = alpha;
+    const float a = (float)alpha;
+    T s = T(0);
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n4; i += (size_t)gridDim.x * blockDim.x) {
+        const float4 xv = __ldg(x + i), pv = __ldg(p + i), rv = __ldg(r + i), av = __ldg(ap + i);
+        float4 v, u;
+        v.x = __fadd_rn(xv.x, __fmul_rn(a, pv.x));
+        v.y = __fadd_rn(xv.y, __fmul_rn(a, pv.y));
+        v.z = __fadd_rn(xv.z, __fmul_rn(a, pv.z));
+        v.w = __fadd_rn(xv.w, __fmul_rn(a, pv.w));
+        xn[i] = v;
+        u.x = __fsub_rn(rv.x, __fmul_rn(a, av.x));
+        u.y = __fsub_rn(rv.y, __fmul_rn(a, av.y));
+        u.z = __fsub_rn(rv.z, __fmul_rn(a, av.z));
+        u.w = __fsub_rn(rv.w, __fmul_rn(a, av.w));
+        rn[i] = u;
+        s += (T)dot4(u, u);
+    }
+    finish_pairs<T>(s, T(0), partials, scal + S_RNRN, scal);
+}
+
 // flags[s] = 1 when any element of float4 segment s (32 float4) of m is non-zero.
 __global__ void segment_flags(const float4 *__restrict__ m, size_t n4, unsigned char *__restrict__ flags) {
     const size_t nseg = (n4 + 31) / 32;
@@ -558,6 +589,20 @@ extern "C" int msn_cg_residual(const float *d_r, const float *d_ap, double *d_sc
     MSN_RED_LAUNCH(cg_residual, kRedGrid, kRedThreads, st, (const float4 *)d_r, (const float4 *)d_ap, d_scal, (float4 *)d_rn,
                                                   n / 4, partials);
     return check_launch("cg_residual");
+}
+
+extern "C" int msn_cg_step(const float *d_x, const float *d_p, const float *d_r, const float *d_ap, double *d_scal,
+                           float *d_xn, float *d_rn, size_t n, void *d_work, size_t work_bytes, void *stream) {
+    clear_error();
+    if (!d_x || !d_p || !d_r || !d_ap || !d_scal || !d_xn || !d_rn) return set_error(MSN_ERR_INVALID, "msn_cg_step: null pointer");
+    if (n % 4 || !aligned16(d_x) || !aligned16(d_p) || !aligned16(d_r) || !aligned16(d_ap) || !aligned16(d_xn) ||
+        !aligned16(d_rn))
+        return set_error(MSN_ERR_INVALID, "msn_cg_step: length must be a multiple of 4, pointers 16-byte aligned");
+    MSN_TRY(check_red_ws(d_work, work_bytes, "msn_cg_step"));
+    cudaStream_t st = as_stream(stream);
+    MSN_RED_LAUNCH(cg_step, kRedGrid, kRedThreads, st, (const float4 *)d_x, (const float4 *)d_p, (const float4 *)d_r,
+                   (const float4 *)d_ap, d_scal, (float4 *)d_xn, (float4 *)d_rn, n / 4, (double *)d_work);
+    return check_launch("cg_step");
 }
 
 extern "C" int msn_cg_direction(const float *d_rn, float *d_p, const double *d_scal, size_t n, void *stream) {

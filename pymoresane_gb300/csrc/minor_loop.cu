@@ -101,11 +101,14 @@ __global__ void minor_control(MinorState *s, const double *snr2, double *hist, i
 
 // p = rn + beta p (main.py:411, the arithmetic of msn_cg_direction), r = rn,
 // and x = xn when the control kernel kept this iteration's xn.
+// r.r of the next iteration is this iteration's rn.rn (r = rn; same values, same
+// reduction order), so it is carried in the scalar block instead of recomputed.
 __global__ void direction_commit(const float4 *__restrict__ rn, float4 *__restrict__ p, float4 *__restrict__ r,
                                  const float4 *__restrict__ xn, float4 *__restrict__ x,
-                                 const double *__restrict__ scal, const MinorState *__restrict__ s, size_t n4) {
+                                 double *__restrict__ scal, const MinorState *__restrict__ s, size_t n4) {
     const float b = (float)scal[S_BETA];
     const bool commit = s->commit != 0;
+    if (blockIdx.x == 0 && threadIdx.x == 0) scal[S_RR] = scal[S_RNRN];
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n4; i += (size_t)gridDim.x * blockDim.x) {
         const float4 rv = __ldg(rn + i);
         float4 pv = p[i];
@@ -259,6 +262,8 @@ int build_graph(Engine *e, const msn_minor_args *a, CacheEntry *ce) {
         MSN_TRY(check_cuda(cudaMemsetAsync(a->ms, 0, (size_t)planes * nvec * sizeof(float), st), "zero sources"));
         MSN_TRY(check_cuda(cudaMemcpyAsync(a->r, a->rec, nvec * sizeof(float), cudaMemcpyDeviceToDevice, st), "r"));
         MSN_TRY(check_cuda(cudaMemcpyAsync(a->p, a->rec, nvec * sizeof(float), cudaMemcpyDeviceToDevice, st), "p"));
+        // r.r of the first iteration (later ones are carried from rn.rn)
+        MSN_TRY(msn_dot2(a->r, a->r, nullptr, nullptr, nvec, a->scal + S_RR, a->red_work, a->red_work_bytes, st));
         // the extraction mask is fixed for the whole minor loop: flag its non-empty segments and
         // rows once, and clear Q, whose rows outside the mask are then never written again
         MSN_TRY(msn_segment_flags(a->emask, (size_t)planes * nvec, a->seg_flags, st));
@@ -279,9 +284,11 @@ int build_graph(Engine *e, const msn_minor_args *a, CacheEntry *ce) {
     long long branch_kernels = 0;
     MSN_TRY(capture_into(e->cs[1], body, &ce->body_kernels, [&](cudaStream_t st) -> int {
         MSN_TRY(apply_a(a, a->p, a->ap, st));
-        MSN_TRY(msn_dot2(a->r, a->r, a->p, a->ap, nvec, a->scal, a->red_work, a->red_work_bytes, st));
-        MSN_TRY(msn_cg_alpha_x(a->x, a->p, a->scal, a->xn, nvec, a->neg, st));
+        // p.Ap into scal[S_PAP] (the second output, scal[S_ALPHA], is rewritten right after);
+        // r.r is carried from the previous iteration (direction_commit) or the prologue
+        MSN_TRY(msn_dot2(a->p, a->ap, nullptr, nullptr, nvec, a->scal + S_PAP, a->red_work, a->red_work_bytes, st));
         if (a->enforce_positivity) {
+            MSN_TRY(msn_cg_alpha_x(a->x, a->p, a->scal, a->xn, nvec, a->neg, st));
             positivity_gate<<<1, 1, 0, st>>>(a->neg, state, if_h);
             MSN_TRY(check_launch("positivity_gate"));
             cudaGraph_t branch = nullptr;
@@ -290,12 +297,17 @@ int build_graph(Engine *e, const msn_minor_args *a, CacheEntry *ce) {
                 MSN_TRY(msn_cg_positivity(a->x, a->xn, a->p, a->scal, nvec, bst));
                 return apply_a(a, a->p, a->ap, bst);
             }));
+        } else {
+            // xn = x + alpha p and rn = r - alpha Ap (with rn.rn, beta) in one pass
+            MSN_TRY(msn_cg_step(a->x, a->p, a->r, a->ap, a->scal, a->xn, a->rn, nvec, a->red_work,
+                                a->red_work_bytes, st));
         }
         MSN_TRY(msn_snr_update_masked(a->esrc, a->ms, a->planes, a->scal, (size_t)planes * nvec, a->seg_flags,
                                       a->snr2, a->red_work, a->red_work_bytes, st));
         minor_control<<<1, 1, 0, st>>>(state, a->snr2, hist, kHistory, while_h);
         MSN_TRY(check_launch("minor_control"));
-        MSN_TRY(msn_cg_residual(a->r, a->ap, a->scal, a->rn, nvec, a->red_work, a->red_work_bytes, st));
+        if (a->enforce_positivity)
+            MSN_TRY(msn_cg_residual(a->r, a->ap, a->scal, a->rn, nvec, a->red_work, a->red_work_bytes, st));
         direction_commit<<<ew_grid4(nvec / 4), 256, 0, st>>>(
             (const float4 *)a->rn, (float4 *)a->p, (float4 *)a->r, (const float4 *)a->xn, (float4 *)a->x, a->scal,
             state, nvec / 4);

@@ -180,6 +180,18 @@ def test_cg_vector_kernels(cuda):
     clamped = np.where(want < 0, np.float32(0), want)
     assert np.array_equal(xpos.cpu().numpy(), clamped)
     assert np.array_equal(ppos.cpu().numpy(), (clamped - x) / af)
+    # the fused step equals cg_alpha_x followed by cg_residual bit for bit (vectors and scalars)
+    scal2 = torch.zeros(8, dtype=torch.float64, device="cuda")
+    scal2[0:2] = scal[0:2]
+    xn2, rn2 = torch.empty_like(xn), torch.empty_like(rn)
+    _native.call("msn_cg_step", t["x"].data_ptr(), t["p"].data_ptr(), t["r"].data_ptr(), t["ap"].data_ptr(),
+                 scal2.data_ptr(), xn2.data_ptr(), rn2.data_ptr(), n, work.data_ptr(), work.numel(), st)
+    assert torch.equal(xn2, xn) and torch.equal(rn2, rn)
+    assert torch.equal(scal2[2:5], scal[2:5])
+    # r.r of the next iteration equals this iteration's rn.rn bit for bit (carried in the minor loop)
+    rr_next = torch.zeros(2, dtype=torch.float64, device="cuda")
+    dev.dot2(rn.reshape(-1), rn.reshape(-1), out=rr_next, work=work)
+    assert rr_next[0].item() == scal[3].item()
 
 
 def test_region_std_and_model_update(cuda):
