@@ -106,11 +106,13 @@ int msn_recompose_row_activity(const unsigned char *d_row_flags, int planes, int
 int msn_iuwt_recompose_rows(const float *d_detail, int planes, const unsigned char *d_act, float *d_out, int ny,
                             int nx, int scale_adjust, void *d_work, size_t work_bytes, void *stream);
 
-/* msn_iuwt_recompose_rows without the zero writes: rows that d_act marks
- * inactive are neither computed nor written. The caller guarantees that they
- * already hold zeros in d_out and in planes 2 and 3 of the workspace (clear
- * both once, e.g. with cudaMemsetAsync, before the calls that share one
+/* msn_iuwt_recompose_rows with almost no zero writes: rows that d_act marks
+ * inactive at every level are neither computed nor written, so the caller
+ * must keep them at zero in d_out and in planes 2 and 3 of the workspace
+ * (clear both once, e.g. with cudaMemsetAsync, before the calls that share one
  * activity map; transforms sharing the workspace only use its planes 0 and 1).
+ * Rows that one call's lower levels made non-zero are re-zeroed by the next
+ * call's higher levels where those are inactive.
  * No counterpart in the reference (the minor loop's A p, main.py:375-384,
  * applied to a detail stack that is zero outside the mask rows). */
 int msn_iuwt_recompose_active_rows(const float *d_detail, int planes, const unsigned char *d_act, float *d_out,

@@ -87,14 +87,17 @@ template <int EPI>
 __global__ void __launch_bounds__(kThreads)
 atrous_band(const float *__restrict__ in, float *__restrict__ out, const float *__restrict__ aux,
             const float *__restrict__ mask, int ny, int nx, int d, int band_rows,
-            const unsigned char *__restrict__ row_flags, int skip_inactive) {
+            const unsigned char *__restrict__ row_flags, int skip_inactive,
+            const unsigned char *__restrict__ zero_rows) {
     extern __shared__ float4 smem4[];
     // masked detail with row flags: rows whose mask row is empty are left as they are (zero)
     if (EPI == kDetailMask && row_flags && band_rows == 1 && !row_flags[blockIdx.x]) return;
     // recomposition with row activity: an inactive output row is exactly zero (all its
     // taps and its detail row are zero), so it is written as zeros without reading anything
     if ((EPI == kAdd || EPI == kStore) && row_flags && band_rows == 1 && !row_flags[blockIdx.x]) {
-        if (skip_inactive) return;  // the caller keeps inactive rows at zero
+        // skip mode: only rows in zero_rows need zeros (they may hold a previous call's values);
+        // every other inactive row is kept at zero by the caller
+        if (skip_inactive && !(zero_rows && zero_rows[blockIdx.x])) return;
         float4 *o4 = reinterpret_cast<float4 *>(out) + (size_t)blockIdx.x * (nx >> 2);
         for (int j = threadIdx.x; j < (nx >> 2); j += blockDim.x) o4[j] = make_float4(0.f, 0.f, 0.f, 0.f);
         return;
@@ -262,9 +265,13 @@ __global__ void zero_plus(const float4 *__restrict__ w, float4 *__restrict__ out
 // rec = 0 + w on the rows act marks active (one row per CTA); inactive rows are
 // not touched (the caller keeps them at zero).
 __global__ void zero_plus_rows(const float4 *__restrict__ w, float4 *__restrict__ out, int nx4,
-                               const unsigned char *__restrict__ act) {
-    if (!act[blockIdx.x]) return;
+                               const unsigned char *__restrict__ act, const unsigned char *__restrict__ zero_rows) {
     const size_t base = (size_t)blockIdx.x * nx4;
+    if (!act[blockIdx.x]) {
+        if (zero_rows && zero_rows[blockIdx.x])
+            for (int j = threadIdx.x; j < nx4; j += blockDim.x) out[base + j] = make_float4(0.f, 0.f, 0.f, 0.f);
+        return;
+    }
     for (int j = threadIdx.x; j < nx4; j += blockDim.x) {
         float4 v = __ldg(w + base + j);
         v.x = __fadd_rn(0.0f, v.x);
@@ -284,7 +291,8 @@ int band_rows_for(int, int) { return 1; }
 
 template <int EPI>
 int launch_band(const float *in, float *out, const float *aux, int ny, int nx, int d, cudaStream_t st,
-                const float *mask = nullptr, const unsigned char *row_flags = nullptr, int skip_inactive = 0) {
+                const float *mask = nullptr, const unsigned char *row_flags = nullptr, int skip_inactive = 0,
+                const unsigned char *zero_rows = nullptr) {
     static std::once_flag once;
     std::call_once(once, [] {
         cudaFuncSetAttribute(atrous_band<EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxSmem);
@@ -295,7 +303,8 @@ int launch_band(const float *in, float *out, const float *aux, int ny, int nx, i
     const int work4 = band * (nx >> 2);
     const int cta = tune_value(kKnobIuwtThreads);  // 64, 128 or 256 (<= kThreads)
     const int threads = work4 >= cta ? cta : ((work4 + 31) / 32) * 32;
-    atrous_band<EPI><<<grid, threads, smem, st>>>(in, out, aux, mask, ny, nx, d, band, row_flags, skip_inactive);
+    atrous_band<EPI><<<grid, threads, smem, st>>>(in, out, aux, mask, ny, nx, d, band, row_flags, skip_inactive,
+                                                   zero_rows);
     return check_launch("atrous_band");
 }
 
@@ -354,8 +363,9 @@ int iuwt_smooth_detail(const float *in, const float *c0, float *w, int ny, int n
     return launch_band<kDetail>(in, w, c0, ny, nx, 1 << scale, st);
 }
 int iuwt_smooth_add(const float *in, const float *w, float *out, int ny, int nx, int scale, cudaStream_t st,
-                    const unsigned char *row_act = nullptr, int skip_inactive = 0) {
-    return launch_band<kAdd>(in, out, w, ny, nx, 1 << scale, st, nullptr, row_act, skip_inactive);
+                    const unsigned char *row_act = nullptr, int skip_inactive = 0,
+                    const unsigned char *zero_rows = nullptr) {
+    return launch_band<kAdd>(in, out, w, ny, nx, 1 << scale, st, nullptr, row_act, skip_inactive, zero_rows);
 }
 int iuwt_smooth_detail_mask(const float *in, const float *c0, const float *mask, float *w, int ny, int nx, int scale,
                             cudaStream_t st, const unsigned char *row_flags = nullptr) {
@@ -452,9 +462,14 @@ int iuwt_decompose_impl(const float *d_in, float *d_detail, float *d_smoothed, i
 // d_act (may be null): [max_scale][ny] bytes, row r of the level of scale s is
 // active when d_act[s * ny + r] != 0 (msn_recompose_row_activity); inactive rows
 // are written as zeros without being computed.
-// skip_inactive (with d_act, no smoothed plane): inactive rows are neither
-// computed nor written; the caller guarantees they already hold zeros in d_out
-// and in p0 / p1 (msn_iuwt_recompose_active_rows).
+// skip_inactive (with d_act, no smoothed plane): inactive rows are not computed.
+// The levels alternate between p0 and p1, and activity only grows from the top
+// level down, so a row a level leaves inactive can hold a value only if a lower
+// level writing the same plane made it active (in an earlier call). Each level
+// therefore writes zeros on the rows active at the lowest level of its plane but
+// inactive at its own, and touches no other inactive row; the caller guarantees
+// that rows never active anywhere hold zeros in p0, p1 and d_out
+// (msn_iuwt_recompose_active_rows).
 int iuwt_recompose_impl(const float *d_detail, int planes, const float *d_smoothed, float *d_out, int ny, int nx,
                         int scale_adjust, float *p0, float *p1, cudaStream_t st,
                         const unsigned char *d_act = nullptr, int skip_inactive = 0) {
@@ -468,19 +483,26 @@ int iuwt_recompose_impl(const float *d_detail, int planes, const float *d_smooth
         nb = (cur_buf == 0) ? 1 : 0;
         return (op == total - 1) ? d_out : bufs[nb];
     };
+    // lowest level (scale) written to each plane: ops alternate p0, p1 and the last op writes d_out
+    int low_scale[2] = {-1, -1};
+    for (int k = 0; k < total - 1; ++k) low_scale[k & 1] = max_scale - 1 - k;
+    auto zero_rows_for = [&](float *dst, int nb) -> const unsigned char * {
+        if (!skip_inactive || dst == d_out || low_scale[nb] < 0) return nullptr;
+        return d_act + (size_t)low_scale[nb] * ny;
+    };
     for (int s = max_scale - 1; s >= scale_adjust; --s, ++op) {
         int nb;
         float *dst = dst_for(nb);
         const float *w = d_detail + (size_t)(s - scale_adjust) * plane;
         if (cur == nullptr && skip_inactive) {
             zero_plus_rows<<<ny, 128, 0, st>>>(reinterpret_cast<const float4 *>(w), reinterpret_cast<float4 *>(dst),
-                                               nx / 4, d_act + (size_t)s * ny);
+                                               nx / 4, d_act + (size_t)s * ny, zero_rows_for(dst, nb));
             MSN_TRY(check_launch("zero_plus_rows"));
         } else if (cur == nullptr) {
             MSN_TRY(launch_zero_plus(w, dst, plane, st));
         } else {
             MSN_TRY(iuwt_smooth_add(cur, w, dst, ny, nx, s, st, d_act ? d_act + (size_t)s * ny : nullptr,
-                                    skip_inactive));
+                                    skip_inactive, zero_rows_for(dst, nb)));
         }
         cur = dst;
         cur_buf = (dst == d_out) ? -1 : nb;
@@ -492,7 +514,7 @@ int iuwt_recompose_impl(const float *d_detail, int planes, const float *d_smooth
             MSN_TRY(check_cuda(cudaMemsetAsync(dst, 0, plane * sizeof(float), st), "zero plane"));
         } else if (d_act) {
             MSN_TRY(launch_band<kStore>(cur, dst, nullptr, ny, nx, 1 << s, st, nullptr, d_act + (size_t)s * ny,
-                                        skip_inactive));
+                                        skip_inactive, zero_rows_for(dst, nb)));
         } else {
             MSN_TRY(iuwt_smooth(cur, dst, ny, nx, s, st));
         }
