@@ -238,8 +238,7 @@ __device__ __forceinline__ void last_pass_store(const float2 *__restrict__ buf, 
 // has Ns = M / R on 16-element blocks (every plan with at least two passes).
 template <int M>
 constexpr bool direct_ok() {
-    return P<M>::NP >= 2 && P<M>::plan.ns[0] == 1 && 16 % P<M>::plan.radix[0] == 0 &&
-           (M / P<M>::plan.radix[P<M>::NP - 1]) % 16 == 0;
+    return direct_ok(P<M>::plan, M);
 }
 
 // --------------------------------------------------------------------------

@@ -81,6 +81,13 @@ __host__ __device__ constexpr CtPlan ct_plan(int m) {
     return p;
 }
 
+// Whether the plan of length m runs the global-fed / global-stored ("direct")
+// kernels: a first pass with Ns = 1 and a radix dividing 16, and a last pass
+// with Ns = M / R on 16-element blocks (every plan with at least two passes).
+__host__ __device__ constexpr bool direct_ok(const CtPlan &p, int m) {
+    return p.ok && p.np >= 2 && p.ns[0] == 1 && 16 % p.radix[0] == 0 && (m / p.radix[p.np - 1]) % 16 == 0;
+}
+
 // Per-length entry points (defined in fft_kernels.cuh, instantiated in fft_inst_*.cu).
 template <int M>
 int conv_run(const float *x, int n, const float2 *spec, float *out, int linear, float2 *t1, float2 *t2,

@@ -25,7 +25,7 @@ int main() {
             if (q > 0) tw += p.ns[q] * (p.radix[q] - 1);
             prod *= p.radix[q];
         }
-        const bool direct = p.np >= 2 && p.ns[0] == 1 && 16 % p.radix[0] == 0 && (m / p.radix[p.np - 1]) % 16 == 0;
+        const bool direct = direct_ok(p, m);   // the predicate the kernels use
         std::printf("%d %d %ld %d %d %d %d %d %d\n", m, p.ok, prod, p.twlen == tw, twbase_ok, p.e, p.fusable, direct,
                     p.w == m / 2 + 1 && p.groups * p.group >= p.w);
     }
