@@ -392,15 +392,16 @@ sq_rows_fwd(const float *__restrict__ x, const __grid_constant__ CUtensorMap lo_
         for (int k1 = 0; k1 < R; ++k1) buf[k1 * PADR + t] = v[tslot(k1)];
         __syncthreads();
 #pragma unroll
-        for (int n1 = 0; n1 < R; ++n1) v[tslot(n1)] = buf[t * PADR + n1];
+        for (int n1 = 0; n1 < R; ++n1) v[n1] = buf[t * PADR + n1];
         __syncthreads();
-        dft64<false, true>(v);  // Z[t + 64 k2] in slot k2
+        dft64<false, false>(v);  // Z[t + 64 k2] in slot tslot(k2)
 #pragma unroll
         for (int k2 = 0; k2 < R; ++k2) {
             const int k = t + R * k2;
-            if (k <= HALF) *reinterpret_cast<float2 *>(out_lo + slot_off(k)) = v[k2];
-            if (k >= HALF) *reinterpret_cast<float2 *>(out_hi + slot_off(M - k)) = v[k2];
-            if (k == 0) *reinterpret_cast<float2 *>(out_hi) = v[k2];
+            const float2 z = v[tslot(k2)];
+            if (k <= HALF) *reinterpret_cast<float2 *>(out_lo + slot_off(k)) = z;
+            if (k >= HALF) *reinterpret_cast<float2 *>(out_hi + slot_off(M - k)) = z;
+            if (k == 0) *reinterpret_cast<float2 *>(out_hi) = z;
         }
         fence_proxy_async();
         __syncthreads();
@@ -512,7 +513,7 @@ sq_cols_conv(float2 *lo, float2 *hi, const float2 *__restrict__ h) {
             for (int k1 = 0; k1 < R; ++k1) buf[k1 * PADR + t] = v[tslot(k1)];
             team_sync(team);
 #pragma unroll
-            for (int n1 = 0; n1 < R; ++n1) v[tslot(n1)] = buf[t * PADR + n1];
+            for (int n1 = 0; n1 < R; ++n1) v[n1] = buf[t * PADR + n1];
             __syncthreads();  // both teams have read their exchange
             if (leader) {
                 fence_proxy_async();
@@ -525,25 +526,30 @@ sq_cols_conv(float2 *lo, float2 *hi, const float2 *__restrict__ h) {
                     bulk_load(in_hi, hi + (size_t)gn * PAIRS * 2, kBlockBytes, bar_in);
                 }
             }
-            dft64<false, true>(v);  // thread t now holds X[t + 64 k2] in slot k2
+            dft64<false, false>(v);  // thread t now holds X[t + 64 k2] in slot tslot(k2)
             if (it == 0) {
                 if (!wait_all(bar_h, parity)) {
                     fail = true;
                     break;
                 }
-                // conj(X * H), with H for row m = t + 64 k2 of this column
+                // conj(X * H), with H for row m = t + 64 k2 of this column, written in natural
+                // order (slot k2): the inverse pass A takes its input in natural order, so one
+                // transform body serves all four passes
+                float2 u[R];
 #pragma unroll
                 for (int k2 = 0; k2 < R; ++k2) {
                     const float2 hv = h_s[(t + R * k2) * 2 + c];
-                    const float2 x = v[k2];
-                    v[k2] = make_float2(x.x * hv.x - x.y * hv.y, -(x.x * hv.y + x.y * hv.x));
+                    const float2 x = v[tslot(k2)];
+                    u[k2] = make_float2(x.x * hv.x - x.y * hv.y, -(x.x * hv.y + x.y * hv.x));
                 }
+#pragma unroll
+                for (int k2 = 0; k2 < R; ++k2) v[k2] = u[k2];
                 __syncthreads();  // the PSF block is consumed: the area is the exchange again
             }
         }
         if (fail) break;
         parity ^= 1u;
-        // v holds conj(y) for y the inverse column transform; position n = t + 64 k2 is
+        // v holds conj(y) in slot tslot(k2) for y the inverse column transform; position n = t + 64 k2 is
         // output row i = (n - 3M/4) mod M; rows i < M/2 are kept:
         // i = t + 64 (k2 - 48) for k2 >= 48 and t + 64 k2 + M/4 for k2 < 16, pair i / 2
         const bool edge = k == 0 || k == HALF;  // c2r uses only the real part of these bins
@@ -551,7 +557,7 @@ sq_cols_conv(float2 *lo, float2 *hi, const float2 *__restrict__ h) {
         for (int k2 = 0; k2 < R; ++k2) {
             if (k2 >= J0 && k2 < J1) continue;
             const int at = ((t >> 1) + (R / 2) * (k2 >= J1 ? k2 - J1 : k2 + J0)) * 2 + c;
-            float2 own = make_float2(v[k2].x, -v[k2].y);
+            float2 own = make_float2(v[tslot(k2)].x, -v[tslot(k2)].y);
             float2 other;
             other.x = __shfl_xor_sync(0xffffffffu, own.x, 1);
             other.y = __shfl_xor_sync(0xffffffffu, own.y, 1);
@@ -643,16 +649,16 @@ sq_rows_inv(const __grid_constant__ CUtensorMap lo_map, const __grid_constant__ 
         for (int k1 = 0; k1 < R; ++k1) buf[k1 * PADR + t] = v[tslot(k1)];
         __syncthreads();
 #pragma unroll
-        for (int n1 = 0; n1 < R; ++n1) v[tslot(n1)] = buf[t * PADR + n1];
+        for (int n1 = 0; n1 < R; ++n1) v[n1] = buf[t * PADR + n1];
         __syncthreads();
-        dft64<true, true>(v);  // z[t + 64 k2] in slot k2
+        dft64<true, false>(v);  // z[t + 64 k2] in slot tslot(k2)
         constexpr float scale = 1.0f / ((float)M * (float)M);  // a power of two: exact
 #pragma unroll
         for (int k2 = 0; k2 < R; ++k2) {
             if (k2 >= J0 && k2 < J1) continue;
             const int c = t + R * (k2 >= J1 ? k2 - J1 : k2 + J0);
-            out_s[c] = v[k2].x * scale;
-            out_s[HALF + c] = v[k2].y * scale;
+            out_s[c] = v[tslot(k2)].x * scale;
+            out_s[HALF + c] = v[tslot(k2)].y * scale;
         }
         fence_proxy_async();
         __syncthreads();
