@@ -699,8 +699,12 @@ template <int M>
 int conv_run(const float *x, int n, const float2 *spec, float *out, int linear, float2 *t1, float2 *t2,
              cudaStream_t st) {
     if constexpr (M == sq::kLength) {
-        // the 2048^2 linear convolution with a 4096^2 PSF: four-step kernels
-        if (linear && n == M / 2 && tune_value(kKnobFourStep)) return sq::conv_run(x, spec, out, t1, t2, st);
+        // the 2048^2 linear convolution with a 4096^2 PSF: four-step kernels. Their bulk and
+        // tensor copies need 16-byte aligned image, spectrum, output and workspace addresses;
+        // other pointers take the Stockham kernels below (same results within rounding).
+        const bool aligned = aligned16(x) && aligned16(spec) && aligned16(out) && aligned16(t1) && aligned16(t2);
+        if (linear && n == M / 2 && aligned && tune_value(kKnobFourStep))
+            return sq::conv_run(x, spec, out, t1, t2, st);
     }
     const int off = linear ? (M - n) / 2 : 0;
     const int shift = (off + M / 2) % M;

@@ -137,3 +137,24 @@ def test_full_size_convolution_2048_dense_random(cuda):
     ref = OC.fft_convolve(x.astype(np.float64), np.fft.rfft2(psf.astype(np.float64)), "linear")
     got = G.fft_convolve(x, dev.psf_spectrum(psf), "gpu", "linear")
     assert np.max(np.abs(got - ref)) <= CONV_TOL * np.max(np.abs(ref))
+
+
+def test_unaligned_pointers_take_the_stockham_path(cuda):
+    # the four-step kernels' bulk copies need 16-byte aligned addresses; an image, output or
+    # spectrum that is only 8-byte aligned is convolved by the Stockham kernels instead
+    from pymoresane_gb300 import _native
+    rng = np.random.default_rng(77)
+    x = rng.standard_normal((2048, 2048)).astype(np.float32)
+    spec = dev.psf_spectrum(make_psf(4096, 3000, rng))
+    ref = dev.fft_convolve(torch.from_numpy(x).cuda(), spec)
+    base = torch.empty(2048 * 2048 + 4, dtype=torch.float32, device="cuda")
+    xu = base[2:2 + 2048 * 2048]                         # 8 bytes past a 16-byte boundary
+    xu.copy_(torch.from_numpy(x).cuda().reshape(-1))
+    assert xu.data_ptr() % 16 == 8
+    obase = torch.empty(2048 * 2048 + 4, dtype=torch.float32, device="cuda")
+    ou = obase[2:2 + 2048 * 2048]
+    work = dev.fft_workspace(2048, 4096, xu.device)
+    _native.call("msn_fft_convolve", xu.data_ptr(), 2048, 4096, spec.packed.data_ptr(), ou.data_ptr(), 1,
+                 work.data_ptr(), work.numel(), dev.stream_handle())
+    got = ou.reshape(2048, 2048)
+    assert torch.max(torch.abs(got - ref)).item() <= 1e-5 * torch.max(torch.abs(ref)).item()
