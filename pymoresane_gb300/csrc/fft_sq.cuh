@@ -585,21 +585,24 @@ sq_cols_conv(float2 *lo, float2 *hi, const float2 *__restrict__ h) {
 
 // 3. Inverse row transforms of the packed pairs; writes rows 2p, 2p + 1 of the
 // n x n output (columns through the shift and crop), scaled by 1 / M^2.
-// Persistent one-team CTAs: the next pair's lo and hi rows arrive by TMA tensor
-// loads into IN while the current pair is transformed; the two output rows
-// (16 KB, contiguous) leave as one bulk store from the exchange buffer.
-constexpr size_t kRowInvSmem = kTeamArea + 2 * kRowSlots + 16 + kTabElems * sizeof(float2);
+// Persistent one-team CTAs. A pair's lo and hi rows arrive by TMA tensor loads
+// into the exchange buffer; once the exchange has been read, the next pair's rows
+// are loaded there while the current pair's second pass runs. The two output rows
+// (16 KB, contiguous) leave as one bulk store from a buffer of their own.
+constexpr unsigned kRowOutBytes = 2 * HALF * sizeof(float);
+constexpr size_t kRowInvSmem = kTeamArea + kRowOutBytes + 16 + kTabElems * sizeof(float2);
+static_assert(2 * kRowSlots <= kTeamArea, "a pair's lo and hi rows fit in the exchange buffer");
 
-__global__ void __launch_bounds__(R, 3)
+__global__ void __launch_bounds__(R, 4)
 sq_rows_inv(const __grid_constant__ CUtensorMap lo_map, const __grid_constant__ CUtensorMap hi_map,
             float *__restrict__ out) {
     extern __shared__ __align__(128) float2 smem[];
     const int t = threadIdx.x;
     const bool leader = t == 0;
     float2 *buf = smem;
-    float *out_s = reinterpret_cast<float *>(smem);  // rows 2p, 2p + 1 after the exchange
-    char *in_lo = reinterpret_cast<char *>(smem) + kTeamArea, *in_hi = in_lo + kRowSlots;
-    uint64_t *bar = reinterpret_cast<uint64_t *>(in_hi + kRowSlots);
+    char *in_lo = reinterpret_cast<char *>(smem), *in_hi = in_lo + kRowSlots;
+    float *out_s = reinterpret_cast<float *>(reinterpret_cast<char *>(smem) + kTeamArea);
+    uint64_t *bar = reinterpret_cast<uint64_t *>(reinterpret_cast<char *>(smem) + kTeamArea + kRowOutBytes);
     float2 *tab = reinterpret_cast<float2 *>(bar + 2);
     __shared__ int ok;
     if (leader) {
@@ -636,13 +639,8 @@ sq_rows_inv(const __grid_constant__ CUtensorMap lo_map, const __grid_constant__ 
             v[j] = j < R / 2 ? *reinterpret_cast<const float2 *>(in_lo + slot_off(n))
                              : *reinterpret_cast<const float2 *>(in_hi + slot_off(M - n));
         }
-        if (leader) bulk_wait_read_all();  // the previous pair's output rows have left the area
-        __syncthreads();                   // IN consumed
-        const int pn = p + gridDim.x;
-        if (leader && pn < PAIRS) {
-            fence_proxy_async();
-            issue(pn);
-        }
+        if (leader) bulk_wait_read_all();  // the previous pair's output rows have left OUT
+        __syncthreads();                   // IN consumed: the buffer becomes the exchange
         dft64<true, false>(v);
         twiddle_tab<true, true>(v, tab, t);
 #pragma unroll
@@ -650,7 +648,12 @@ sq_rows_inv(const __grid_constant__ CUtensorMap lo_map, const __grid_constant__ 
         __syncthreads();
 #pragma unroll
         for (int n1 = 0; n1 < R; ++n1) v[n1] = buf[t * PADR + n1];
-        __syncthreads();
+        __syncthreads();                   // the exchange is read: the next pair's rows may land
+        const int pn = p + gridDim.x;
+        if (leader && pn < PAIRS) {
+            fence_proxy_async();
+            issue(pn);
+        }
         dft64<true, false>(v);  // z[t + 64 k2] in slot tslot(k2)
         constexpr float scale = 1.0f / ((float)M * (float)M);  // a power of two: exact
 #pragma unroll
@@ -663,7 +666,7 @@ sq_rows_inv(const __grid_constant__ CUtensorMap lo_map, const __grid_constant__ 
         fence_proxy_async();
         __syncthreads();
         if (leader) {
-            bulk_store(out + (size_t)(2 * p) * HALF, out_s, 2 * HALF * sizeof(float));
+            bulk_store(out + (size_t)(2 * p) * HALF, out_s, kRowOutBytes);
             bulk_commit();
         }
     }
