@@ -253,12 +253,16 @@ int msn_label(const float *d_img, int ny, int nx, int *d_labels, int *d_count, v
 size_t msn_reduce_workspace_bytes(void);
 
 /* Accumulation type of every reduction of the library (CG inner products,
- * SNR norms, residual statistics), process-wide: 64 (float64 accumulation of
- * float32 four-element partials, the default) or 32 (plain float32
- * accumulation). The float32 setting exists to state the error of a plain
- * float32 path against the float64 one; the reference's GPU path reduces on
- * the host in its arrays' precision (pymoresane/main.py:386-411). Minor-loop
- * graphs are cached per setting. Returns MSN_ERR_INVALID for other values. */
+ * SNR norms, residual statistics), process-wide:
+ *   64 (default): float32 four-element partials accumulated in float64;
+ *   48: the same partials accumulated in float-float pairs (about 48
+ *       significant bits, float32 pipes only) within each CTA and in float64
+ *       across CTAs; faster on GB300, whose float64 rate is low;
+ *   32: plain float32 accumulation.
+ * The 48 and 32 settings exist for the precision comparison; the reference's
+ * GPU path reduces on the host in its arrays' precision
+ * (pymoresane/main.py:386-411). Minor-loop graphs are cached per setting.
+ * Returns MSN_ERR_INVALID for other values. */
 int msn_set_reduction_precision(int bits);
 int msn_reduction_precision(void);
 

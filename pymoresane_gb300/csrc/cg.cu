@@ -21,22 +21,60 @@ constexpr int kRedThreads = 256;
 
 enum { S_RR = 0, S_PAP = 1, S_ALPHA = 2, S_RNRN = 3, S_BETA = 4 };
 
-// Accumulation type of the reductions: double (default) or float (the plain
-// float32 variant selected with msn_set_reduction_precision(32), kept for the
-// float32-versus-float64 error comparison).
+// A float-float number: the unevaluated sum hi + lo of two floats, |lo| <= ulp(hi)/2.
+// Additions keep their rounding error with Knuth's TwoSum (every operation a
+// separately rounded float32 add, no contraction), so a running sum carries about
+// 48 significant bits while using only the float32 pipes. GB300's float64 rate is
+// a small fraction of its float32 rate, and float64 per-thread accumulation made
+// each reduction over a 2048^2 vector about 9 us slower than float32.
+struct FF {
+    float hi, lo;
+    FF() = default;  // trivial, so FF can live in __shared__ arrays; FF() value-initialises to zero
+    __device__ __forceinline__ explicit FF(float v) : hi(v), lo(0.0f) {}
+    __device__ __forceinline__ explicit FF(int v) : hi((float)v), lo(0.0f) {}
+    __device__ __forceinline__ explicit FF(double v) : hi((float)v), lo((float)(v - (double)(float)v)) {}
+    __device__ __forceinline__ explicit operator double() const { return (double)hi + (double)lo; }
+    __device__ __forceinline__ FF &operator+=(const FF &b) {
+        // TwoSum of the high parts, then the low parts, then a fast renormalisation
+        const float s = __fadd_rn(hi, b.hi);
+        const float bb = __fsub_rn(s, hi);
+        const float e = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(b.hi, bb));
+        const float t = __fadd_rn(e, __fadd_rn(lo, b.lo));
+        hi = __fadd_rn(s, t);
+        lo = __fsub_rn(t, __fsub_rn(hi, s));
+        return *this;
+    }
+};
+
+__device__ __forceinline__ float shfl_xor(float v, int off) { return __shfl_xor_sync(0xffffffffu, v, off); }
+__device__ __forceinline__ double shfl_xor(double v, int off) { return __shfl_xor_sync(0xffffffffu, v, off); }
+__device__ __forceinline__ FF shfl_xor(FF v, int off) {
+    FF r;
+    r.hi = __shfl_xor_sync(0xffffffffu, v.hi, off);
+    r.lo = __shfl_xor_sync(0xffffffffu, v.lo, off);
+    return r;
+}
+
+// Accumulation type of the reductions within a CTA: FF (float-float, the
+// default), double (msn_set_reduction_precision(64)) or float (the plain float32
+// variant, 32); the sum across CTAs is float64 except in the float32 variant.
 template <class T>
 __device__ __forceinline__ T block_sum(T v) {
     __shared__ T sh[32];
-    for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+    for (int off = 16; off > 0; off >>= 1) v += shfl_xor(v, off);
     if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
     __syncthreads();
     const int nw = blockDim.x >> 5;
     v = threadIdx.x < nw ? sh[threadIdx.x] : T(0);
     if (threadIdx.x < 32)
-        for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+        for (int off = 16; off > 0; off >>= 1) v += shfl_xor(v, off);
     __syncthreads();
     return v;  // valid in thread 0
 }
+
+// Type of the sum across CTAs: float for the plain float32 variant, double otherwise.
+template <class T> struct CrossSum { using type = double; };
+template <> struct CrossSum<float> { using type = float; };
 
 // Two-stage deterministic reduction in one launch: every CTA writes its
 // partial pair, and the last CTA to finish (completion counter after the
@@ -46,24 +84,25 @@ __device__ __forceinline__ T block_sum(T v) {
 template <class T>
 __device__ __forceinline__ bool finish_pairs(T s0, T s1, double *__restrict__ partials, double *out,
                                              double *beta_scal) {
+    using X = typename CrossSum<T>::type;
     __shared__ bool last;
-    __shared__ T ws[2][kRedThreads / 32];
+    __shared__ X ws[2][kRedThreads / 32];
     s0 = block_sum(s0);
     s1 = block_sum(s1);
     unsigned *counter = reinterpret_cast<unsigned *>(partials + 2 * kRedGrid);
     if (threadIdx.x == 0) {
-        partials[2 * blockIdx.x] = s0;
-        partials[2 * blockIdx.x + 1] = s1;
+        partials[2 * blockIdx.x] = (double)s0;
+        partials[2 * blockIdx.x + 1] = (double)s1;
         __threadfence();
         last = atomicAdd(counter, 1u) == gridDim.x - 1;
     }
     __syncthreads();
     if (!last) return false;
     const int t = threadIdx.x;
-    T a = T(0), b = T(0);
+    X a = X(0), b = X(0);
     for (int k = t; k < (int)gridDim.x; k += kRedThreads) {
-        a += (T)__ldcg(partials + 2 * k);
-        b += (T)__ldcg(partials + 2 * k + 1);
+        a += (X)__ldcg(partials + 2 * k);
+        b += (X)__ldcg(partials + 2 * k + 1);
     }
     for (int off = 16; off > 0; off >>= 1) {
         a += __shfl_xor_sync(0xffffffffu, a, off);
@@ -75,8 +114,8 @@ __device__ __forceinline__ bool finish_pairs(T s0, T s1, double *__restrict__ pa
     }
     __syncthreads();
     if (t < 32) {
-        a = t < kRedThreads / 32 ? ws[0][t] : T(0);
-        b = t < kRedThreads / 32 ? ws[1][t] : T(0);
+        a = t < kRedThreads / 32 ? ws[0][t] : X(0);
+        b = t < kRedThreads / 32 ? ws[1][t] : X(0);
         for (int off = 16; off > 0; off >>= 1) {
             a += __shfl_xor_sync(0xffffffffu, a, off);
             b += __shfl_xor_sync(0xffffffffu, b, off);
@@ -115,7 +154,30 @@ __global__ void __launch_bounds__(kRedThreads)
 dual_partials(const float4 *__restrict__ a, const float4 *__restrict__ b, const float4 *__restrict__ c,
               const float4 *__restrict__ d, size_t n4, double *__restrict__ partials, double *__restrict__ out) {
     T s0 = T(0), s1 = T(0);
-    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n4; i += (size_t)gridDim.x * blockDim.x) {
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    // Four grid-stride steps per round with all their loads issued first (memory-level
+    // parallelism); the terms are added in the same order as one step at a time.
+    for (; i + 3 * stride < n4; i += 4 * stride) {
+        float4 va[4], vb[4], vc[4], vd[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            va[u] = __ldg(a + i + u * stride);
+            vb[u] = __ldg(b + i + u * stride);
+            if (DIFF || c) vc[u] = __ldg(c + i + u * stride);
+            if (!DIFF && c) vd[u] = __ldg(d + i + u * stride);
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            s0 += (T)dot4(va[u], vb[u]);
+            if (DIFF) {
+                s1 += (T)sqdiff4(va[u], vc[u]);
+            } else if (c) {
+                s1 += (T)dot4(vc[u], vd[u]);
+            }
+        }
+    }
+    for (; i < n4; i += stride) {
         const float4 va = __ldg(a + i);
         s0 += (T)dot4(va, __ldg(b + i));
         if (DIFF) {
@@ -146,9 +208,10 @@ snr_partials_f64(const double *__restrict__ a, const double *__restrict__ b, siz
 // warp-shuffle tree per warp, then one over the warp sums.
 constexpr int kFinalizeThreads = ((kRedGrid + 31) / 32) * 32;
 
-template <class T>
+template <class T0>
 __global__ void __launch_bounds__(kFinalizeThreads)
 finalize_pairs(const double *__restrict__ partials, double *__restrict__ out) {
+    using T = typename CrossSum<T0>::type;
     __shared__ T ws[2][kFinalizeThreads / 32];
     const int t = threadIdx.x;
     T a = t < kRedGrid ? (T)partials[2 * t] : T(0);
@@ -425,13 +488,16 @@ bool reduce_fp32() { return g_reduce_bits.load(std::memory_order_relaxed) == 32;
 
 namespace {
 
-// Launches kernel template K<..., T> with T = float or double as selected.
+// Launches kernel template K<..., T> with T = FF, double or float as selected.
 #define MSN_RED_LAUNCH(KERNEL, GRID, BLOCK, ST, ...)                       \
     do {                                                                   \
-        if (reduce_fp32())                                                 \
+        const int bits_ = g_reduce_bits.load(std::memory_order_relaxed);   \
+        if (bits_ == 32)                                                   \
             KERNEL<float><<<GRID, BLOCK, 0, ST>>>(__VA_ARGS__);            \
-        else                                                               \
+        else if (bits_ == 64)                                              \
             KERNEL<double><<<GRID, BLOCK, 0, ST>>>(__VA_ARGS__);           \
+        else                                                               \
+            KERNEL<FF><<<GRID, BLOCK, 0, ST>>>(__VA_ARGS__);               \
     } while (0)
 
 int ew_grid(size_t n) {
@@ -451,15 +517,19 @@ int dual_reduce(const float *a, const float *b, const float *c, const float *d, 
     if (n % 4 || !aligned16(a) || !aligned16(b) || !aligned16(c) || !aligned16(d))
         return set_error(MSN_ERR_INVALID, "reduction: length must be a multiple of 4 and pointers 16-byte aligned");
     const float4 *a4 = (const float4 *)a, *b4 = (const float4 *)b, *c4 = (const float4 *)c, *d4 = (const float4 *)d;
-    const bool f32 = reduce_fp32();
-    if (diff && f32)
+    const int bits = g_reduce_bits.load(std::memory_order_relaxed);
+    if (diff && bits == 32)
         dual_partials<true, float><<<kRedGrid, kRedThreads, 0, st>>>(a4, b4, c4, d4, n / 4, partials, out);
-    else if (diff)
+    else if (diff && bits == 64)
         dual_partials<true, double><<<kRedGrid, kRedThreads, 0, st>>>(a4, b4, c4, d4, n / 4, partials, out);
-    else if (f32)
+    else if (diff)
+        dual_partials<true, FF><<<kRedGrid, kRedThreads, 0, st>>>(a4, b4, c4, d4, n / 4, partials, out);
+    else if (bits == 32)
         dual_partials<false, float><<<kRedGrid, kRedThreads, 0, st>>>(a4, b4, c4, d4, n / 4, partials, out);
-    else
+    else if (bits == 64)
         dual_partials<false, double><<<kRedGrid, kRedThreads, 0, st>>>(a4, b4, c4, d4, n / 4, partials, out);
+    else
+        dual_partials<false, FF><<<kRedGrid, kRedThreads, 0, st>>>(a4, b4, c4, d4, n / 4, partials, out);
     return check_launch("dual_partials");
 }
 
@@ -668,8 +738,8 @@ extern "C" int msn_region_std(const float *d_img, int pitch, int rows, int cols,
 
 extern "C" int msn_set_reduction_precision(int bits) {
     clear_error();
-    if (bits != 32 && bits != 64)
-        return set_error(MSN_ERR_INVALID, "msn_set_reduction_precision: bits must be 32 or 64, got %d", bits);
+    if (bits != 32 && bits != 48 && bits != 64)
+        return set_error(MSN_ERR_INVALID, "msn_set_reduction_precision: bits must be 32, 48 or 64, got %d", bits);
     g_reduce_bits.store(bits);
     return MSN_OK;
 }

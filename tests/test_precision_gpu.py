@@ -5,9 +5,10 @@ the reference's float32 casts removed) run on the seeded 2048^2 problem
 (4096^2 PSF, scale_count=7) for three major iterations; its result is the
 fixture tests/golden/oracle_f64_2048_m3.npz (tests/golden/make_golden.py).
 
-The GPU path runs twice on the same input: with the library's default
-reductions (float64 accumulation of float32 partials) and with plain float32
-accumulation (msn_set_reduction_precision(32)). For each, the test states the
+The GPU path runs three times on the same input: with the library's default
+reductions (float64 accumulation of float32 partials), with float-float
+accumulation within each CTA (msn_set_reduction_precision(48)) and with plain
+float32 accumulation (msn_set_reduction_precision(32)). For each, the test states the
 model error (max |model - oracle| / peak), the residual RMS error (relative)
 and whether the per-major decisions match the oracle's; the wavelet
 coefficients of the dirty image (GPU float32 decomposition against the float64
@@ -33,6 +34,7 @@ import cases as mg  # noqa: E402
 
 MODEL_TOL = 1e-4
 RMS_TOL = 1e-4
+NAMES = {64: "float64", 48: "float-float", 32: "float32"}
 
 
 def oracle_fixture():
@@ -64,7 +66,7 @@ def test_float32_vs_float64_reductions_against_fp64_oracle(cuda):
     ref_rms = float(g["residual_rms"])
     ref_recs = [tuple(int(v) for v in r) for r in g["records"]]
     stats = {}
-    for bits in (64, 32):
+    for bits in (64, 48, 32):
         img = run(dirty, psf, bits)
         recs = [(r["max_scale"], r["scale_adjust"], r["minor"], int(r["reverted"])) for r in img.log]
         rms = float(np.sqrt(np.mean(np.square(img.residual.astype(np.float64)))))
@@ -76,19 +78,23 @@ def test_float32_vs_float64_reductions_against_fp64_oracle(cuda):
     w64 = OI.decompose(dirty.astype(np.float64), 7, 0, arith="f64")
     coef = float(np.max(np.abs(w32 - w64))) / float(np.max(np.abs(w64)))
     print(f"\nerror vs float64 oracle (2048^2, 3 major iterations): wavelet coefficients {coef:.2e} of peak; "
-          + "; ".join(f"{'float64' if b == 64 else 'float32'} reductions: model {s['model']:.2e} of peak, "
+          + "; ".join(f"{NAMES[b]} reductions: model {s['model']:.2e} of peak, "
                       f"residual RMS {s['rms']:.2e} relative, decisions {'identical' if s['decisions'] else 'differ'}"
                       for b, s in stats.items()))
     assert coef <= 2e-6
     s64 = stats[64]
     assert s64["decisions"] and s64["model"] <= MODEL_TOL and s64["rms"] <= RMS_TOL
     assert np.isfinite(stats[32]["model"]) and np.isfinite(stats[32]["rms"])
+    assert stats[48]["decisions"] and stats[48]["model"] <= MODEL_TOL
     assert _native.query("msn_reduction_precision") == 64
 
 
 def test_reduction_precision_setting(cuda):
     with pytest.raises(ValueError):
         _native.call("msn_set_reduction_precision", 16)
+    _native.call("msn_set_reduction_precision", 48)
+    assert _native.query("msn_reduction_precision") == 48
+    _native.call("msn_set_reduction_precision", 64)
     assert _native.query("msn_reduction_precision") == 64
 
 
@@ -107,7 +113,7 @@ def test_float32_reductions_on_a_long_run(cuda):
     peak = float(np.max(np.abs(ref)))
     ref_majors = int(g["major"])
     out = {}
-    for bits in (64, 32):
+    for bits in (64, 48, 32):
         _native.call("msn_set_reduction_precision", bits)
         try:
             img = DataImage(dirty, psf, None, 1.0, 1.0)
@@ -117,6 +123,6 @@ def test_float32_reductions_on_a_long_run(cuda):
         out[bits] = (float(np.max(np.abs(img.model - ref))) / peak, len(img.log),
                      sum(r["minor"] for r in img.log))
     print(f"\n512^2 run to completion against the reference ({ref_majors} major iterations): "
-          + "; ".join(f"{'float64' if b == 64 else 'float32'} reductions: model {e:.2e} of peak, {mj} major / "
+          + "; ".join(f"{NAMES[b]} reductions: model {e:.2e} of peak, {mj} major / "
                       f"{mn} minor iterations" for b, (e, mj, mn) in out.items()))
     assert out[64][0] <= 2e-4 and abs(out[64][1] - ref_majors) <= 1
