@@ -81,14 +81,21 @@ template <> struct CrossSum<float> { using type = float; };
 // partials, reset to zero by that CTA) sums the kRedGrid pairs in a fixed
 // order -- thread t adds pairs t, t + 256, t + 512, then warp-shuffle trees --
 // so the totals do not depend on which CTA finishes last.
+// cta_has_work == 0 (uniform across the CTA): every thread's sums are the +0 they
+// started from, so the block sums (+0) are written without being formed.
 template <class T>
 __device__ __forceinline__ bool finish_pairs(T s0, T s1, double *__restrict__ partials, double *out,
-                                             double *beta_scal) {
+                                             double *beta_scal, int cta_has_work = 1) {
     using X = typename CrossSum<T>::type;
     __shared__ bool last;
     __shared__ X ws[2][kRedThreads / 32];
-    s0 = block_sum(s0);
-    s1 = block_sum(s1);
+    if (cta_has_work) {
+        s0 = block_sum(s0);
+        s1 = block_sum(s1);
+    } else {
+        s0 = T(0);
+        s1 = T(0);
+    }
     unsigned *counter = reinterpret_cast<unsigned *>(partials + 2 * kRedGrid);
     if (threadIdx.x == 0) {
         partials[2 * blockIdx.x] = (double)s0;
@@ -256,8 +263,10 @@ snr_update(const float4 *__restrict__ e, float4 *__restrict__ ms, const float4 *
            const unsigned char *__restrict__ seg_flags, double *__restrict__ out) {
     const float a = (float)scal[S_ALPHA];
     T s0 = T(0), s1 = T(0);
+    int worked = 0;
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n4; i += (size_t)gridDim.x * blockDim.x) {
         if (seg_flags && seg_flags[i >> 5] == 0) continue;
+        worked = 1;
         const float4 ev = __ldg(e + i), qv = __ldg(q + i);
         float4 mv = ms[i];
         mv.x = __fadd_rn(mv.x, __fmul_rn(a, qv.x));
@@ -268,7 +277,8 @@ snr_update(const float4 *__restrict__ e, float4 *__restrict__ ms, const float4 *
         s0 += (T)dot4(ev, ev);
         s1 += (T)sqdiff4(ev, mv);
     }
-    finish_pairs<T>(s0, s1, partials, out, nullptr);
+    // most CTAs of the masked pass see no non-empty segment: skip their block sums
+    finish_pairs<T>(s0, s1, partials, out, nullptr, __syncthreads_or(worked));
 }
 
 // The vector updates evaluate the reference's float32 expressions
