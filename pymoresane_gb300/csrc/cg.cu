@@ -264,18 +264,33 @@ snr_update(const float4 *__restrict__ e, float4 *__restrict__ ms, const float4 *
     const float a = (float)scal[S_ALPHA];
     T s0 = T(0), s1 = T(0);
     int worked = 0;
-    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n4; i += (size_t)gridDim.x * blockDim.x) {
-        if (seg_flags && seg_flags[i >> 5] == 0) continue;
-        worked = 1;
-        const float4 ev = __ldg(e + i), qv = __ldg(q + i);
-        float4 mv = ms[i];
-        mv.x = __fadd_rn(mv.x, __fmul_rn(a, qv.x));
-        mv.y = __fadd_rn(mv.y, __fmul_rn(a, qv.y));
-        mv.z = __fadd_rn(mv.z, __fmul_rn(a, qv.z));
-        mv.w = __fadd_rn(mv.w, __fmul_rn(a, qv.w));
-        ms[i] = mv;
-        s0 += (T)dot4(ev, ev);
-        s1 += (T)sqdiff4(ev, mv);
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    // The segment flags of eight grid-stride steps are loaded together: one flag load
+    // per step would make every step wait for the previous one (the pass is almost all
+    // skipped segments). Elements are still visited, and summed, in the same order.
+    constexpr int kAhead = 8;
+    for (size_t i0 = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i0 < n4; i0 += kAhead * stride) {
+        unsigned char f[kAhead];
+#pragma unroll
+        for (int u = 0; u < kAhead; ++u) {
+            const size_t i = i0 + u * stride;
+            f[u] = i < n4 ? (seg_flags ? __ldg(seg_flags + (i >> 5)) : (unsigned char)1) : (unsigned char)0;
+        }
+#pragma unroll
+        for (int u = 0; u < kAhead; ++u) {
+            if (!f[u]) continue;
+            const size_t i = i0 + u * stride;
+            worked = 1;
+            const float4 ev = __ldg(e + i), qv = __ldg(q + i);
+            float4 mv = ms[i];
+            mv.x = __fadd_rn(mv.x, __fmul_rn(a, qv.x));
+            mv.y = __fadd_rn(mv.y, __fmul_rn(a, qv.y));
+            mv.z = __fadd_rn(mv.z, __fmul_rn(a, qv.z));
+            mv.w = __fadd_rn(mv.w, __fmul_rn(a, qv.w));
+            ms[i] = mv;
+            s0 += (T)dot4(ev, ev);
+            s1 += (T)sqdiff4(ev, mv);
+        }
     }
     // most CTAs of the masked pass see no non-empty segment: skip their block sums
     finish_pairs<T>(s0, s1, partials, out, nullptr, __syncthreads_or(worked));
