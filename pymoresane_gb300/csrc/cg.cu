@@ -83,15 +83,17 @@ template <> struct CrossSum<float> { using type = float; };
 // so the totals do not depend on which CTA finishes last.
 // cta_has_work == 0 (uniform across the CTA): every thread's sums are the +0 they
 // started from, so the block sums (+0) are written without being formed.
+// second == 0 (uniform): the second sum is identically +0 (a single dot product or
+// the residual norm), so its block and cross-CTA sums are skipped and +0 written.
 template <class T>
 __device__ __forceinline__ bool finish_pairs(T s0, T s1, double *__restrict__ partials, double *out,
-                                             double *beta_scal, int cta_has_work = 1) {
+                                             double *beta_scal, int cta_has_work = 1, int second = 1) {
     using X = typename CrossSum<T>::type;
     __shared__ bool last;
     __shared__ X ws[2][kRedThreads / 32];
     if (cta_has_work) {
         s0 = block_sum(s0);
-        s1 = block_sum(s1);
+        s1 = second ? block_sum(s1) : T(0);
     } else {
         s0 = T(0);
         s1 = T(0);
@@ -109,11 +111,11 @@ __device__ __forceinline__ bool finish_pairs(T s0, T s1, double *__restrict__ pa
     X a = X(0), b = X(0);
     for (int k = t; k < (int)gridDim.x; k += kRedThreads) {
         a += (X)__ldcg(partials + 2 * k);
-        b += (X)__ldcg(partials + 2 * k + 1);
+        if (second) b += (X)__ldcg(partials + 2 * k + 1);
     }
     for (int off = 16; off > 0; off >>= 1) {
         a += __shfl_xor_sync(0xffffffffu, a, off);
-        b += __shfl_xor_sync(0xffffffffu, b, off);
+        if (second) b += __shfl_xor_sync(0xffffffffu, b, off);
     }
     if ((t & 31) == 0) {
         ws[0][t >> 5] = a;
@@ -125,7 +127,7 @@ __device__ __forceinline__ bool finish_pairs(T s0, T s1, double *__restrict__ pa
         b = t < kRedThreads / 32 ? ws[1][t] : X(0);
         for (int off = 16; off > 0; off >>= 1) {
             a += __shfl_xor_sync(0xffffffffu, a, off);
-            b += __shfl_xor_sync(0xffffffffu, b, off);
+            if (second) b += __shfl_xor_sync(0xffffffffu, b, off);
         }
         if (t == 0) {
             out[0] = (double)a;
@@ -193,7 +195,7 @@ dual_partials(const float4 *__restrict__ a, const float4 *__restrict__ b, const 
             s1 += (T)dot4(__ldg(c + i), __ldg(d + i));
         }
     }
-    finish_pairs<T>(s0, s1, partials, out, nullptr);
+    finish_pairs<T>(s0, s1, partials, out, nullptr, 1, DIFF || c != nullptr);
 }
 
 // Float64 inputs: partials of sum a^2 and sum (a - b)^2 with every product and
@@ -353,7 +355,7 @@ cg_residual(const float4 *__restrict__ r, const float4 *__restrict__ ap, double 
         s += (T)dot4(v, v);
     }
     // scal[S_RNRN] = rn.rn, scal[S_BETA] = rn.rn / r.r
-    finish_pairs<T>(s, T(0), partials, scal + S_RNRN, scal);
+    finish_pairs<T>(s, T(0), partials, scal + S_RNRN, scal, 1, 0);
 }
 
 // One pass of the step without positivity: xn = x + alpha p and rn = r - alpha Ap
@@ -384,7 +386,7 @@ cg_step(const float4 *__restrict__ x, const float4 *__restrict__ p, const float4
         rn[i] = u;
         s += (T)dot4(u, u);
     }
-    finish_pairs<T>(s, T(0), partials, scal + S_RNRN, scal);
+    finish_pairs<T>(s, T(0), partials, scal + S_RNRN, scal, 1, 0);
 }
 
 // flags[s] = 1 when any element of float4 segment s (32 float4) of m is non-zero.
