@@ -273,7 +273,9 @@ int msn_reduction_precision(void);
  *   fft_sq_fwd_ctas, fft_sq_col_ctas, fft_sq_inv_ctas
  *                    0..8: resident CTAs per SM of the three four-step kernels
  *                    (0: as many as fit)
- *   iuwt_threads     64, 128 or 256: threads per CTA of the a trous passes
+ *   iuwt_threads     64, 128 or 256: threads per CTA of the a trous passes on
+ *                    rows of up to 2048 floats
+ *   iuwt_threads_wide  the same for wider rows
  * Results do not depend on them. Changing one invalidates cached minor-loop
  * graphs. No counterpart in the reference (which fixes its launch shapes,
  * 32 x 32 blocks, pymoresane/iuwt.py:452-460). */

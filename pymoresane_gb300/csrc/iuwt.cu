@@ -301,7 +301,7 @@ int launch_band(const float *in, float *out, const float *aux, int ny, int nx, i
     const size_t smem = (size_t)band * nx * sizeof(float);
     const int grid = (ny + band - 1) / band;
     const int work4 = band * (nx >> 2);
-    const int cta = tune_value(kKnobIuwtThreads);  // 64, 128 or 256 (<= kThreads)
+    const int cta = tune_value(nx <= 2048 ? kKnobIuwtThreads : kKnobIuwtThreadsWide);  // 64, 128 or 256
     const int threads = work4 >= cta ? cta : ((work4 + 31) / 32) * 32;
     atrous_band<EPI><<<grid, threads, smem, st>>>(in, out, aux, mask, ny, nx, d, band, row_flags, skip_inactive,
                                                    zero_rows);
@@ -319,7 +319,7 @@ int launch_pair(const float *in, const float *c0, const float *mask, float *w, f
         cudaFuncSetAttribute(atrous_pair<MASK>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxSmem);
     });
     const int nx4 = nx >> 2;
-    const int cta = tune_value(kKnobIuwtThreads);  // 64, 128 or 256 (<= kThreads)
+    const int cta = tune_value(nx <= 2048 ? kKnobIuwtThreads : kKnobIuwtThreadsWide);  // 64, 128 or 256
     const int threads = nx4 >= cta ? cta : ((nx4 + 31) / 32) * 32;
     atrous_pair<MASK><<<ny, threads, 2 * (size_t)nx * sizeof(float), st>>>(in, c0, mask, w, next, ny, nx, d,
                                                                             row_flags);

@@ -27,7 +27,15 @@ inline int check_launch(const char *what) {
 
 // Tunable launch parameters (tune.cu): the current value of a knob, and an
 // epoch that changes whenever any knob does.
-enum Knob { kKnobFourStep = 0, kKnobSqFwdCtas, kKnobSqColCtas, kKnobSqInvCtas, kKnobIuwtThreads, kKnobCount };
+enum Knob {
+    kKnobFourStep = 0,
+    kKnobSqFwdCtas,
+    kKnobSqColCtas,
+    kKnobSqInvCtas,
+    kKnobIuwtThreads,      // a trous CTA size for rows of up to 2048 floats
+    kKnobIuwtThreadsWide,  // ... for wider rows
+    kKnobCount
+};
 int tune_value(Knob k);
 unsigned tune_epoch();
 

@@ -25,10 +25,11 @@ constexpr KnobSpec kSpecs[kKnobCount] = {
     {"fft_sq_fwd_ctas", 0, 0, 8, 0},   // resident CTAs per SM of the four-step row kernels (0: as many as fit)
     {"fft_sq_col_ctas", 0, 0, 8, 0},   // ... of the four-step column kernel
     {"fft_sq_inv_ctas", 0, 0, 8, 0},   // ... of the four-step inverse row kernel
-    {"iuwt_threads", 256, 64, 256, 1}, // threads per CTA of the a trous passes (one image row per CTA)
+    {"iuwt_threads", 256, 64, 256, 1},      // threads per CTA of the a trous passes, rows of <= 2048 floats
+    {"iuwt_threads_wide", 256, 64, 256, 1}, // ... rows of more than 2048 floats
 };
 
-std::atomic<int> g_values[kKnobCount] = {{1}, {0}, {0}, {0}, {256}};
+std::atomic<int> g_values[kKnobCount] = {{1}, {0}, {0}, {0}, {256}, {256}};
 std::atomic<unsigned> g_epoch{0};
 
 int find(const char *name) {

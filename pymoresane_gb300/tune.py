@@ -4,7 +4,8 @@ The library reads a few tunable launch parameters at every launch (declared
 with msn_tune_set in include/msn.h): which kernels run the 2048^2 linear
 convolution with a 4096^2 PSF (the four-step kernels or the Stockham ones),
 how many CTAs of each four-step kernel share an SM, and how many threads a CTA
-of the a trous passes has. None of them changes a result; they only change the
+of the a trous passes has (one value for rows of up to 2048 floats, one for wider
+rows). None of them changes a result; they only change the
 speed, and the best values depend on the device.
 
 ``autotune()`` times the candidates of each parameter on the real operation
@@ -29,13 +30,14 @@ import threading
 from . import _native
 
 CACHE_ENV = "PYMORESANE_GB300_TUNE_CACHE"
-KNOBS = ("fft_four_step", "fft_sq_fwd_ctas", "fft_sq_col_ctas", "fft_sq_inv_ctas", "iuwt_threads")
+KNOBS = ("fft_four_step", "fft_sq_fwd_ctas", "fft_sq_col_ctas", "fft_sq_inv_ctas", "iuwt_threads", "iuwt_threads_wide")
 CANDIDATES = {
     "fft_four_step": (1, 0),
     "fft_sq_fwd_ctas": (0, 2, 3),
     "fft_sq_col_ctas": (0, 2),
     "fft_sq_inv_ctas": (0, 2),
     "iuwt_threads": (256, 128, 64),
+    "iuwt_threads_wide": (256, 128, 64),
 }
 _applied = False
 _lock = threading.Lock()
@@ -156,17 +158,30 @@ def autotune(n=2048, reps=10, path=None, save=True):
         dev.iuwt_recompose(w, 0, smoothed=c, out=rec, work=iwork)
 
     times = {}
+    tuned = {}
     for name in KNOBS:
+        # the convolution parameters only matter for the 2048^2 / 4096^2 case the
+        # four-step kernels serve; the a trous CTA size for this problem's row width
+        if name.startswith("fft_") and n != 2048:
+            continue
         if name.startswith("fft_sq_") and get("fft_four_step") == 0:
             continue
-        op = iuwt if name == "iuwt_threads" else conv
+        if name == ("iuwt_threads_wide" if n <= 2048 else "iuwt_threads"):
+            continue
+        op = iuwt if name.startswith("iuwt_") else conv
         best, t = choose(name, CANDIDATES[name], _timer(op, reps))
         times[name] = {str(k): v for k, v in t.items()}
+        tuned[name] = best
     torch.cuda.synchronize()
-    result = {"device": device_key(), "n": n, "values": current(), "times_s": times}
+    result = {"device": device_key(), "n": n, "values": current(), "tuned": tuned, "times_s": times}
     if save:
+        # one entry per device; each run updates only the parameters it tuned
         data = load_cache(path)
-        data[device_key()] = result
+        entry = data.get(device_key(), {})
+        values = dict(entry.get("values", {}))
+        values.update(tuned)
+        data[device_key()] = {"device": device_key(), "values": values,
+                              "runs": dict(entry.get("runs", {}), **{str(n): {"tuned": tuned, "times_s": times}})}
         save_cache(data, path)
     return result
 

@@ -13,7 +13,7 @@ def _reset_knobs():
 
 def test_registry_defaults_ranges_and_epoch():
     assert tune.current() == {"fft_four_step": 1, "fft_sq_fwd_ctas": 0, "fft_sq_col_ctas": 0, "fft_sq_inv_ctas": 0,
-                              "iuwt_threads": 256}
+                              "iuwt_threads": 256, "iuwt_threads_wide": 256}
     e0 = _native.query("msn_tune_epoch")
     tune.set_values({"iuwt_threads": 128})
     assert tune.get("iuwt_threads") == 128 and _native.query("msn_tune_epoch") != e0

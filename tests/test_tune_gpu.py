@@ -19,7 +19,9 @@ def test_autotune_choices_do_not_change_results(cuda, tmp_path):
         w_ref = dev.iuwt_decompose(x, 6, 0)[0].clone()
         res = tune.autotune(n=2048, reps=3, path=str(tmp_path / "tune.json"))
         assert set(res["values"]) == set(tune.KNOBS)
-        assert tune.load_cache(str(tmp_path / "tune.json"))[tune.device_key()]["values"] == res["values"]
+        assert "iuwt_threads_wide" not in res["tuned"] and "fft_four_step" in res["tuned"]
+        cached = tune.load_cache(str(tmp_path / "tune.json"))[tune.device_key()]["values"]
+        assert all(cached[k] == v for k, v in res["tuned"].items())
         # every candidate of every knob gives the same convolution (within the FFT tolerance) and the
         # same wavelet coefficients (bit for bit)
         for four_step in (0, 1):
@@ -31,5 +33,11 @@ def test_autotune_choices_do_not_change_results(cuda, tmp_path):
         for threads in (64, 128, 256):
             tune.set_values({"iuwt_threads": threads})
             assert torch.equal(dev.iuwt_decompose(x, 6, 0)[0], w_ref)
+        # wide rows have their own parameter
+        xw = torch.from_numpy(rng.standard_normal((64, 4096)).astype(np.float32)).cuda()
+        ww_ref = dev.iuwt_decompose(xw, 5, 0)[0].clone()
+        for threads in (64, 128, 256):
+            tune.set_values({"iuwt_threads_wide": threads})
+            assert torch.equal(dev.iuwt_decompose(xw, 5, 0)[0], ww_ref)
     finally:
         tune.reset()
