@@ -303,7 +303,7 @@ def run_deconv(args, rank, world, dist):
     for _ in range(args.warmup):
         eng, model, residual = step()
     torch.cuda.synchronize()
-    traj = (len(eng.log), sum(r.get("minor", 0) for r in eng.log))
+    traj = (len(eng.log), eng.minor_total)  # every minor loop, also those a major iteration restarts
 
     sampler = ClockSampler(gpu_uuid()) if rank == 0 else None
     if sampler:
@@ -536,7 +536,7 @@ def main():
             dirty, psf = deconv_problem(0)
             ref = reference_trajectory()
             traj, source = (ref, "the reference's own complete run of this problem") if ref else \
-                ((90, 1409), "this implementation's complete run of this problem on GB300 (reference run not recorded)")
+                ((90, 1595), "this implementation's complete run of this problem on GB300 (reference run not recorded)")
         # Each step is a bounded sample of seconds; warm-up samples are untimed. The run stops
         # taking samples after about 150 s (at least one timed sample), so that it ends in minutes.
         t_run = time.perf_counter()

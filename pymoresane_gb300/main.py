@@ -158,6 +158,7 @@ class Deconvolver:
         self.psf_data_shape = tuple(self.psf.shape)
         self.dirty_data_shape = dirty_shape
         self.log = []
+        self.minor_total = 0  # minor iterations over every minor loop run so far
         self.complete = False
         # True: keep mask * W(H x) as a running sum (ms += alpha * mask * W(H p), exact by
         # linearity) instead of recomputing mask * W(H xn) with a convolution and a
@@ -310,6 +311,7 @@ class Deconvolver:
         _native.call("msn_moresane_run", engine, ctypes.byref(a), ctypes.byref(res), records, cap, events,
                      len(events), st)
         _replay(events[:res.n_events])
+        self.minor_total += sum(e.a for e in events[:res.n_events] if e.code == _native.EV_MINOR_DONE)
         for r in records[:res.n_records]:
             self.log.append({"major": r.major, "max_scale": r.max_scale, "scale_adjust": r.scale_adjust,
                              "minor": r.minor, "snr": r.snr, "std": r.std, "reverted": bool(r.reverted)})
@@ -526,6 +528,7 @@ class Deconvolver:
                         V["x"], V["xn"] = xn, x
                         x, xn = xn, x
                 have_x = True
+                self.minor_total += minor
                 logger.info("%d minor loop iterations performed.", minor)
                 rec.update(max_scale=max_scale, scale_adjust=scale_adjust, minor=minor, snr=snr_current)
                 if minor == minor_loop_miter and snr_current > 10.5:

@@ -193,7 +193,9 @@ def save_baseline(name, dirty, psf, kw, img, lines, dt, full_residual):
     idx = np.flatnonzero(flat).astype(np.int64)
     n = dirty.shape[0]
     c = slice(n // 2 - 128, n // 2 + 128)
-    out = dict(dirty_sha=digest(dirty), psf_sha=digest(psf), model_idx=idx, model_val=flat[idx],
+    # a model with more than a quarter of its pixels set is smaller stored whole
+    model = dict(model=img.model) if 4 * idx.size > flat.size else dict(model_idx=idx, model_val=flat[idx])
+    out = dict(dirty_sha=digest(dirty), psf_sha=digest(psf), **model,
                model_shape=np.array(img.model.shape), residual_std=np.array(np.std(img.residual)),
                residual_centre=img.residual[c, c], log=np.array(lines), seconds=np.array(dt),
                major=np.array(len(recs)), minor_total=np.array(sum(sum(r["minor"]) for r in recs)),
