@@ -174,6 +174,12 @@ int msn_fft_convolve(const float *d_x, int n, int m, const void *d_spec, float *
  * convolution's output is not valid. No counterpart in the reference. */
 int msn_fft_status(unsigned *out);
 
+/* Grid sizes (persistent CTAs) the four-step 4096-point kernels launch with on the
+ * current device under the current tuning values: out[0] forward rows, out[1]
+ * columns, out[2] inverse rows. Introspection for the autotuner; no counterpart
+ * in the reference. */
+int msn_fft_sq_grids(int *out);
+
 /* Replaces gpu_r2c_fft -- pymoresane/iuwt_convolution.py:76-106:
  * d_out [m][m/2+1] = rfft2(d_in [m][m]). */
 int msn_rfft2(const float *d_in, int m, void *d_out, void *d_work, size_t work_bytes, void *stream);

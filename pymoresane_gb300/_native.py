@@ -41,6 +41,7 @@ SIGNATURES = {
     "msn_spectrum_pack": (c_int, [c_void_p, c_int, c_void_p, c_void_p]),
     "msn_fft_convolve": (c_int, [c_void_p, c_int, c_int, c_void_p, c_void_p, c_int, c_void_p, c_size_t, c_void_p]),
     "msn_fft_status": (c_int, [c_void_p]),
+    "msn_fft_sq_grids": (c_int, [c_void_p]),
     "msn_rfft2": (c_int, [c_void_p, c_int, c_void_p, c_void_p, c_size_t, c_void_p]),
     "msn_irfft2": (c_int, [c_void_p, c_int, c_void_p, c_void_p, c_size_t, c_void_p]),
     "msn_fft_shift": (c_int, [c_void_p, c_int, c_void_p]),

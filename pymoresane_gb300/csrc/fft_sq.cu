@@ -47,3 +47,14 @@ extern "C" int msn_fft_status(unsigned *out) {
     *out = v;
     return MSN_OK;
 }
+
+extern "C" int msn_fft_sq_grids(int *out) {
+    msn::clear_error();
+    if (!out) return msn::set_error(MSN_ERR_INVALID, "msn_fft_sq_grids: null pointer");
+    msn::fftk::sq::SqLaunch c;
+    MSN_TRY(msn::fftk::sq::launch_config(&c));
+    out[0] = c.fwd_grid;
+    out[1] = c.col_grid;
+    out[2] = c.inv_grid;
+    return MSN_OK;
+}

@@ -84,6 +84,13 @@ def current():
     return {k: get(k) for k in KNOBS}
 
 
+def sq_grids():
+    """(forward rows, columns, inverse rows) persistent grids of the four-step kernels on this device."""
+    out = (ctypes.c_int * 3)()
+    _native.call("msn_fft_sq_grids", out)
+    return tuple(out)
+
+
 def set_values(values):
     for k, v in values.items():
         if k in KNOBS:

@@ -29,6 +29,10 @@ def test_autotune_choices_do_not_change_results(cuda, tmp_path):
                 tune.set_values({"fft_four_step": four_step, "fft_sq_col_ctas": ctas, "fft_sq_fwd_ctas": ctas,
                                  "fft_sq_inv_ctas": ctas})
                 got = dev.fft_convolve(x, spec)
+                if four_step:
+                    grids = tune.sq_grids()
+                    sms = torch.cuda.get_device_properties(0).multi_processor_count
+                    assert all(0 < g for g in grids) and (ctas == 0 or max(grids) <= ctas * sms), grids
                 assert torch.max(torch.abs(got - ref)).item() <= 1e-5 * torch.max(torch.abs(ref)).item()
         for threads in (64, 128, 256):
             tune.set_values({"iuwt_threads": threads})
