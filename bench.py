@@ -692,6 +692,9 @@ def main():
     iuwt = measure_iuwt(5, 3, seed=rank)
     conv_us, conv_alg = conv_roofline()
     conv_gbs = conv_alg / (conv_us * 1e-6) / 1e9
+    from pymoresane_gb300 import tune as _tune
+    conv_kernels = ("fft_convolve (four-step sq_rows_fwd + sq_cols_conv + sq_rows_inv)" if _tune.get("fft_four_step")
+                    else "fft_convolve (Stockham rfft_rows + conv_cols + irfft_rows)")
     if rank == 0:
         cpu = None
         if not args.no_cpu_baseline:
@@ -710,8 +713,7 @@ def main():
             "latency_ms": {"p50": percentile(res["lat"], 50), "p99": percentile(res["lat"], 99),
                            "mode": "plain (one image at a time)"},
             "iuwt_gbs": iuwt["gbs"], "iuwt_frac_of_hbm": iuwt["gbs"] / hbm_peak,
-            "roofline": {"bound": "hbm", "kernel": "fft_convolve (rfft_rows + conv_cols + irfft_rows), linear "
-                                                  "2048^2 image / 4096^2 PSF",
+            "roofline": {"bound": "hbm", "kernel": conv_kernels + ", linear 2048^2 image / 4096^2 PSF",
                          "achieved": conv_gbs, "peak": hbm_peak, "peak_kind": peak_kind, "unit": "GB/s",
                          "frac": conv_gbs / hbm_peak, "avg_launch_us": conv_us,
                          "algorithmic_bytes_per_launch": conv_alg,
