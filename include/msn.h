@@ -169,6 +169,15 @@ int msn_spectrum_pack(const void *d_std, int m, void *d_packed, void *stream);
 int msn_fft_convolve(const float *d_x, int n, int m, const void *d_spec, float *d_out, int linear, void *d_work,
                      size_t work_bytes, void *stream);
 
+/* msn_fft_convolve for an input known to be zero outside some rows: d_rows [n]
+ * bytes, d_rows[r] != 0 where row r of d_x may be non-zero (rows flagged zero
+ * must hold zeros). The result equals msn_fft_convolve's (zeros compare equal);
+ * the 2048^2 linear case skips the row transforms of pairs of zero rows. Used
+ * by the minor loop, whose vectors live on the rows of the extraction mask's
+ * dilated support. No counterpart in the reference. */
+int msn_fft_convolve_rows(const float *d_x, int n, int m, const void *d_spec, float *d_out, int linear,
+                          const unsigned char *d_rows, void *d_work, size_t work_bytes, void *stream);
+
 /* Reads and clears the status word of the persistent FFT kernels (synchronous):
  * bit 0 is set when a bounded wait for a bulk copy gave up, in which case the
  * convolution's output is not valid. No counterpart in the reference. */

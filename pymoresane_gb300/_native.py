@@ -40,6 +40,8 @@ SIGNATURES = {
                                  c_void_p]),
     "msn_spectrum_pack": (c_int, [c_void_p, c_int, c_void_p, c_void_p]),
     "msn_fft_convolve": (c_int, [c_void_p, c_int, c_int, c_void_p, c_void_p, c_int, c_void_p, c_size_t, c_void_p]),
+    "msn_fft_convolve_rows": (c_int, [c_void_p, c_int, c_int, c_void_p, c_void_p, c_int, c_void_p, c_void_p, c_size_t,
+                                      c_void_p]),
     "msn_fft_status": (c_int, [c_void_p]),
     "msn_fft_sq_grids": (c_int, [c_void_p]),
     "msn_rfft2": (c_int, [c_void_p, c_int, c_void_p, c_void_p, c_size_t, c_void_p]),

@@ -158,19 +158,25 @@ __device__ __forceinline__ float sqdiff4(const float4 &a, const float4 &b) {
 
 // partials[2*b + 0] = sum a*b, partials[2*b + 1] = sum c*d (or sum (a - c)^2 when DIFF).
 // n4 float4 groups (callers guarantee n % 4 == 0 and 16-byte alignment).
+// With a row support, elements outside it are skipped (their terms are zero).
 template <bool DIFF, class T>
 __global__ void __launch_bounds__(kRedThreads)
 dual_partials(const float4 *__restrict__ a, const float4 *__restrict__ b, const float4 *__restrict__ c,
-              const float4 *__restrict__ d, size_t n4, double *__restrict__ partials, double *__restrict__ out) {
+              const float4 *__restrict__ d, size_t n4, double *__restrict__ partials, double *__restrict__ out,
+              RowSupport sup) {
     T s0 = T(0), s1 = T(0);
     const size_t stride = (size_t)gridDim.x * blockDim.x;
     size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     // Four grid-stride steps per round with all their loads issued first (memory-level
     // parallelism); the terms are added in the same order as one step at a time.
     for (; i + 3 * stride < n4; i += 4 * stride) {
+        bool on[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) on[u] = sup.active(i + u * stride);
         float4 va[4], vb[4], vc[4], vd[4];
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
+            if (!on[u]) continue;
             va[u] = __ldg(a + i + u * stride);
             vb[u] = __ldg(b + i + u * stride);
             if (DIFF || c) vc[u] = __ldg(c + i + u * stride);
@@ -178,6 +184,7 @@ dual_partials(const float4 *__restrict__ a, const float4 *__restrict__ b, const 
         }
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
+            if (!on[u]) continue;
             s0 += (T)dot4(va[u], vb[u]);
             if (DIFF) {
                 s1 += (T)sqdiff4(va[u], vc[u]);
@@ -187,6 +194,7 @@ dual_partials(const float4 *__restrict__ a, const float4 *__restrict__ b, const 
         }
     }
     for (; i < n4; i += stride) {
+        if (!sup.active(i)) continue;
         const float4 va = __ldg(a + i);
         s0 += (T)dot4(va, __ldg(b + i));
         if (DIFF) {
@@ -366,12 +374,14 @@ template <class T>
 __global__ void __launch_bounds__(kRedThreads)
 cg_step(const float4 *__restrict__ x, const float4 *__restrict__ p, const float4 *__restrict__ r,
         const float4 *__restrict__ ap, double *__restrict__ scal, float4 *__restrict__ xn, float4 *__restrict__ rn,
-        size_t n4, double *__restrict__ partials) {
+        size_t n4, double *__restrict__ partials, RowSupport sup) {
     const double alpha = scal[S_RR] / scal[S_PAP];
     if (blockIdx.x == 0 && threadIdx.x == 0) scal[S_ALPHA] = alpha;
     const float a = (float)alpha;
     T s = T(0);
+    // with a row support, xn and rn outside it are left as they are (the caller keeps them zero)
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n4; i += (size_t)gridDim.x * blockDim.x) {
+        if (!sup.active(i)) continue;
         const float4 xv = __ldg(x + i), pv = __ldg(p + i), rv = __ldg(r + i), av = __ldg(ap + i);
         float4 v, u;
         v.x = __fadd_rn(xv.x, __fmul_rn(a, pv.x));
@@ -540,24 +550,43 @@ constexpr size_t kPartialBytes = 2 * kRedGrid * sizeof(double) + 16;
 }  // namespace
 
 int dual_reduce(const float *a, const float *b, const float *c, const float *d, size_t n, bool diff, double *out,
-                double *partials, cudaStream_t st) {
+                double *partials, cudaStream_t st, RowSupport sup = {nullptr, 1u}) {
     if (n % 4 || !aligned16(a) || !aligned16(b) || !aligned16(c) || !aligned16(d))
         return set_error(MSN_ERR_INVALID, "reduction: length must be a multiple of 4 and pointers 16-byte aligned");
     const float4 *a4 = (const float4 *)a, *b4 = (const float4 *)b, *c4 = (const float4 *)c, *d4 = (const float4 *)d;
     const int bits = g_reduce_bits.load(std::memory_order_relaxed);
     if (diff && bits == 32)
-        dual_partials<true, float><<<kRedGrid, kRedThreads, 0, st>>>(a4, b4, c4, d4, n / 4, partials, out);
+        dual_partials<true, float><<<kRedGrid, kRedThreads, 0, st>>>(a4, b4, c4, d4, n / 4, partials, out, sup);
     else if (diff && bits == 64)
-        dual_partials<true, double><<<kRedGrid, kRedThreads, 0, st>>>(a4, b4, c4, d4, n / 4, partials, out);
+        dual_partials<true, double><<<kRedGrid, kRedThreads, 0, st>>>(a4, b4, c4, d4, n / 4, partials, out, sup);
     else if (diff)
-        dual_partials<true, FF><<<kRedGrid, kRedThreads, 0, st>>>(a4, b4, c4, d4, n / 4, partials, out);
+        dual_partials<true, FF><<<kRedGrid, kRedThreads, 0, st>>>(a4, b4, c4, d4, n / 4, partials, out, sup);
     else if (bits == 32)
-        dual_partials<false, float><<<kRedGrid, kRedThreads, 0, st>>>(a4, b4, c4, d4, n / 4, partials, out);
+        dual_partials<false, float><<<kRedGrid, kRedThreads, 0, st>>>(a4, b4, c4, d4, n / 4, partials, out, sup);
     else if (bits == 64)
-        dual_partials<false, double><<<kRedGrid, kRedThreads, 0, st>>>(a4, b4, c4, d4, n / 4, partials, out);
+        dual_partials<false, double><<<kRedGrid, kRedThreads, 0, st>>>(a4, b4, c4, d4, n / 4, partials, out, sup);
     else
-        dual_partials<false, FF><<<kRedGrid, kRedThreads, 0, st>>>(a4, b4, c4, d4, n / 4, partials, out);
+        dual_partials<false, FF><<<kRedGrid, kRedThreads, 0, st>>>(a4, b4, c4, d4, n / 4, partials, out, sup);
     return check_launch("dual_partials");
+}
+
+int dot_rows(const float *a, const float *b, size_t n, RowSupport sup, double *out, void *work, size_t work_bytes,
+             cudaStream_t st) {
+    if (!a || !b || !out || !work || work_bytes < kPartialBytes || !sup.rows || sup.cols4 == 0)
+        return set_error(MSN_ERR_INVALID, "dot_rows: bad arguments");
+    return dual_reduce(a, b, nullptr, nullptr, n, false, out, (double *)work, st, sup);
+}
+
+int cg_step_rows(const float *x, const float *p, const float *r, const float *ap, double *scal, float *xn, float *rn,
+                 size_t n, RowSupport sup, void *work, size_t work_bytes, cudaStream_t st) {
+    if (!x || !p || !r || !ap || !scal || !xn || !rn || !work || work_bytes < kPartialBytes || sup.cols4 == 0)
+        return set_error(MSN_ERR_INVALID, "cg_step_rows: bad arguments");
+    if (n % 4 || !aligned16(x) || !aligned16(p) || !aligned16(r) || !aligned16(ap) || !aligned16(xn) ||
+        !aligned16(rn))
+        return set_error(MSN_ERR_INVALID, "cg_step_rows: length must be a multiple of 4, pointers 16-byte aligned");
+    MSN_RED_LAUNCH(cg_step, kRedGrid, kRedThreads, st, (const float4 *)x, (const float4 *)p, (const float4 *)r,
+                   (const float4 *)ap, scal, (float4 *)xn, (float4 *)rn, n / 4, (double *)work, sup);
+    return check_launch("cg_step");
 }
 
 }  // namespace msn
@@ -698,7 +727,8 @@ extern "C" int msn_cg_step(const float *d_x, const float *d_p, const float *d_r,
     MSN_TRY(check_red_ws(d_work, work_bytes, "msn_cg_step"));
     cudaStream_t st = as_stream(stream);
     MSN_RED_LAUNCH(cg_step, kRedGrid, kRedThreads, st, (const float4 *)d_x, (const float4 *)d_p, (const float4 *)d_r,
-                   (const float4 *)d_ap, d_scal, (float4 *)d_xn, (float4 *)d_rn, n / 4, (double *)d_work);
+                   (const float4 *)d_ap, d_scal, (float4 *)d_xn, (float4 *)d_rn, n / 4, (double *)d_work,
+                   RowSupport{nullptr, 1u});
     return check_launch("cg_step");
 }
 

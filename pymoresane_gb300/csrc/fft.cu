@@ -70,9 +70,9 @@ int get_plan(int m, CtPlan *p, const char *fn) {
 
 #define MSN_CASE_CONV(M) \
     case M:              \
-        return fftk::conv_run<M>(x, n, spec, out, linear, t1, t2, st);
+        return fftk::conv_run<M>(x, n, spec, out, linear, t1, t2, st, rows);
 int dispatch_conv(int m, const float *x, int n, const float2 *spec, float *out, int linear, float2 *t1, float2 *t2,
-                  cudaStream_t st) {
+                  cudaStream_t st, const unsigned char *rows) {
     switch (m) { MSN_FFT_SIZES(MSN_CASE_CONV) }
     return set_error(MSN_ERR_INVALID, "unsupported FFT size %d", m);
 }
@@ -141,9 +141,10 @@ extern "C" int msn_psf_spectrum(const float *d_psf, int rows, int cols, int m, i
                              as_stream(stream));
 }
 
-extern "C" int msn_fft_convolve(const float *d_x, int n, int m, const void *d_spec, float *d_out, int linear,
-                                void *d_work, size_t work_bytes, void *stream) {
-    clear_error();
+namespace msn {
+// msn_fft_convolve with the rows of d_x that may be non-zero (rows[r] != 0, null: all rows).
+int fft_convolve_rows(const float *d_x, int n, int m, const void *d_spec, float *d_out, int linear, void *d_work,
+                      size_t work_bytes, const unsigned char *rows, cudaStream_t st) {
     static const char *fn = "msn_fft_convolve";
     CtPlan pl;
     MSN_TRY(get_plan(m, &pl, fn));
@@ -156,7 +157,21 @@ extern "C" int msn_fft_convolve(const float *d_x, int n, int m, const void *d_sp
         return set_error(MSN_ERR_WORKSPACE, "%s: workspace %zu < %zu", fn, work_bytes, 2 * half);
     float2 *t1 = (float2 *)d_work;
     float2 *t2 = (float2 *)((char *)d_work + half);
-    return dispatch_conv(m, d_x, n, (const float2 *)d_spec, d_out, linear, t1, t2, as_stream(stream));
+    return dispatch_conv(m, d_x, n, (const float2 *)d_spec, d_out, linear, t1, t2, st, rows);
+}
+}  // namespace msn
+
+extern "C" int msn_fft_convolve(const float *d_x, int n, int m, const void *d_spec, float *d_out, int linear,
+                                void *d_work, size_t work_bytes, void *stream) {
+    clear_error();
+    return fft_convolve_rows(d_x, n, m, d_spec, d_out, linear, d_work, work_bytes, nullptr, as_stream(stream));
+}
+
+extern "C" int msn_fft_convolve_rows(const float *d_x, int n, int m, const void *d_spec, float *d_out, int linear,
+                                     const unsigned char *d_rows, void *d_work, size_t work_bytes, void *stream) {
+    clear_error();
+    if (!d_rows) return set_error(MSN_ERR_INVALID, "msn_fft_convolve_rows: null row flags");
+    return fft_convolve_rows(d_x, n, m, d_spec, d_out, linear, d_work, work_bytes, d_rows, as_stream(stream));
 }
 
 extern "C" int msn_rfft2(const float *d_in, int m, void *d_out, void *d_work, size_t work_bytes, void *stream) {

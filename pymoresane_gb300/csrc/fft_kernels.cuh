@@ -697,14 +697,14 @@ int launch_cols(const float2 *in, InL in_lay, int in_rows, int in_off, const flo
 // --------------------------------------------------------------------------
 template <int M>
 int conv_run(const float *x, int n, const float2 *spec, float *out, int linear, float2 *t1, float2 *t2,
-             cudaStream_t st) {
+             cudaStream_t st, const unsigned char *rows) {
     if constexpr (M == sq::kLength) {
         // the 2048^2 linear convolution with a 4096^2 PSF: four-step kernels. Their bulk and
         // tensor copies need 16-byte aligned image, spectrum, output and workspace addresses;
         // other pointers take the Stockham kernels below (same results within rounding).
         const bool aligned = aligned16(x) && aligned16(spec) && aligned16(out) && aligned16(t1) && aligned16(t2);
         if (linear && n == M / 2 && aligned && tune_value(kKnobFourStep))
-            return sq::conv_run(x, spec, out, t1, t2, st);
+            return sq::conv_run(x, spec, out, t1, t2, st, rows);
     }
     const int off = linear ? (M - n) / 2 : 0;
     const int shift = (off + M / 2) % M;
@@ -739,7 +739,7 @@ int irfft2_run(const float2 *in, float *out, float2 *t2, cudaStream_t st) {
 
 #define MSN_FFT_INSTANTIATE(M)                                                                                 \
     template int conv_run<M>(const float *, int, const float2 *, float *, int, float2 *, float2 *,            \
-                             cudaStream_t);                                                                    \
+                             cudaStream_t, const unsigned char *);                                             \
     template int spectrum_run<M>(const float *, int, int, int, int, float2 *, float2 *, cudaStream_t);        \
     template int rfft2_run<M>(const float *, float2 *, float2 *, cudaStream_t);                               \
     template int irfft2_run<M>(const float2 *, float *, float2 *, cudaStream_t);

@@ -89,9 +89,11 @@ __host__ __device__ constexpr bool direct_ok(const CtPlan &p, int m) {
 }
 
 // Per-length entry points (defined in fft_kernels.cuh, instantiated in fft_inst_*.cu).
+// rows (may be null): the rows of x that may be non-zero (rows[r] != 0); the
+// four-step kernels skip the transforms of row pairs that are both zero.
 template <int M>
 int conv_run(const float *x, int n, const float2 *spec, float *out, int linear, float2 *t1, float2 *t2,
-             cudaStream_t st);
+             cudaStream_t st, const unsigned char *rows);
 template <int M>
 int spectrum_run(const float *psf, int rows, int cols, int off_r, int off_c, float2 *out, float2 *t1, cudaStream_t st);
 template <int M>
@@ -104,7 +106,8 @@ namespace sq {
 // group-major with 2 columns per group) by the four-step kernels of
 // fft_sq.cuh; lo / hi: two workspaces of kPlaneElems float2 each.
 constexpr int kLength = 4096;
-int conv_run(const float *x, const float2 *spec, float *out, float2 *lo, float2 *hi, cudaStream_t st);
+int conv_run(const float *x, const float2 *spec, float *out, float2 *lo, float2 *hi, cudaStream_t st,
+             const unsigned char *rows);
 }  // namespace sq
 
 #define MSN_FFT_SIZES(X) \
@@ -113,7 +116,7 @@ int conv_run(const float *x, const float2 *spec, float *out, float2 *lo, float2 
 
 #define MSN_FFT_EXTERN(M)                                                                                      \
     extern template int conv_run<M>(const float *, int, const float2 *, float *, int, float2 *, float2 *,     \
-                                    cudaStream_t);                                                             \
+                                    cudaStream_t, const unsigned char *);                                      \
     extern template int spectrum_run<M>(const float *, int, int, int, int, float2 *, float2 *, cudaStream_t); \
     extern template int rfft2_run<M>(const float *, float2 *, float2 *, cudaStream_t);                       \
     extern template int irfft2_run<M>(const float2 *, float *, float2 *, cudaStream_t);

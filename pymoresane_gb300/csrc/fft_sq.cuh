@@ -341,9 +341,18 @@ constexpr size_t kRowFwdSmem = kTeamArea + kRowInBytes + 16;
 // rows are bulk-copied into IN while the current pair is transformed, and the
 // spectrum rows leave through TMA tensor stores from box slots in the exchange
 // buffer (lo[k] = Z[k] for k <= M/2, hi[c] = Z[(M - c) mod M] for c <= M/2).
+//
+// rows (may be null) flags the image rows that may be non-zero. A pair of zero
+// rows has a zero spectrum: its lo / hi rows are stored as zeros without a
+// transform (the transform of zeros gives zeros, up to the sign of zero). The
+// pairs are then taken from a work list with the pairs that need a transform
+// first, so that those spread evenly over the CTAs.
+constexpr int kPairsPerThread = PAIRS / R;
+static_assert(kPairsPerThread * R == PAIRS && kPairsPerThread <= 32, "work-list scan: whole pairs per thread");
+
 __global__ void __launch_bounds__(R, 4)
 sq_rows_fwd(const float *__restrict__ x, const __grid_constant__ CUtensorMap lo_map,
-            const __grid_constant__ CUtensorMap hi_map) {
+            const __grid_constant__ CUtensorMap hi_map, const unsigned char *__restrict__ rows) {
     extern __shared__ __align__(128) float2 smem[];
     const int t = threadIdx.x;
     const bool leader = t == 0;
@@ -353,55 +362,103 @@ sq_rows_fwd(const float *__restrict__ x, const __grid_constant__ CUtensorMap lo_
     const float *in_b = in_a + HALF;
     uint64_t *bar = reinterpret_cast<uint64_t *>(reinterpret_cast<char *>(smem) + kTeamArea + kRowInBytes);
     __shared__ int ok;
+    __shared__ unsigned short order[PAIRS];
+    __shared__ int warp_total[R / 32];
     if (leader) {
         mbar_init(bar, 1);
         mbar_init_fence();
     }
+    // work list: item i is pair order[i]; items [0, n_work) need a transform
+    int n_work = PAIRS;
+    if (rows) {
+        unsigned m = 0;
+#pragma unroll
+        for (int k = 0; k < kPairsPerThread; ++k) {
+            const int pp = kPairsPerThread * t + k;
+            if (__ldg(rows + 2 * pp) | __ldg(rows + 2 * pp + 1)) m |= 1u << k;
+        }
+        const int c = __popc(m);
+        int inc = c;  // inclusive scan over the warp
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, inc, off);
+            if ((t & 31) >= off) inc += y;
+        }
+        if ((t & 31) == 31) warp_total[t >> 5] = inc;
+        __syncthreads();
+        int before = inc - c;
+        n_work = 0;
+#pragma unroll
+        for (int w = 0; w < R / 32; ++w) {
+            if (w < (t >> 5)) before += warp_total[w];
+            n_work += warp_total[w];
+        }
+        int a = before, z = n_work + (kPairsPerThread * t - before);
+#pragma unroll
+        for (int k = 0; k < kPairsPerThread; ++k) {
+            const int pp = kPairsPerThread * t + k;
+            if ((m >> k) & 1u)
+                order[a++] = (unsigned short)pp;
+            else
+                order[z++] = (unsigned short)pp;
+        }
+    }
     __syncthreads();
-    int p = blockIdx.x;
-    if (leader && p < PAIRS) {
+    auto pair_of = [&](int item) { return rows ? (int)order[item] : item; };
+    int item = blockIdx.x;
+    if (leader && item < n_work) {
         mbar_expect_tx(bar, kRowInBytes);
-        bulk_load((void *)in_a, x + (size_t)(2 * p) * HALF, kRowInBytes, bar);
+        bulk_load((void *)in_a, x + (size_t)(2 * pair_of(item)) * HALF, kRowInBytes, bar);
     }
     unsigned parity = 0;
-    for (; p < PAIRS; p += gridDim.x) {
-        if (leader) ok = mbar_wait(bar, parity);
-        __syncthreads();
-        if (!ok) {
-            if (leader) mbar_wait(bar, parity);
-            break;
-        }
-        if (!leader) mbar_wait(bar, parity);
-        parity ^= 1u;
-        float2 v[R];
+    for (; item < PAIRS; item += gridDim.x) {
+        const int p = pair_of(item);
+        if (item >= n_work) {
+            // a pair of zero rows: zero spectrum rows (the items of a CTA that need a
+            // transform all come before its zero items, so no input copy is pending)
+            if (leader) bulk_wait_read_all();  // the previous pair's spectrum rows have left the area
+            __syncthreads();
+            float4 *z4 = reinterpret_cast<float4 *>(smem);
+            for (int k = t; k < (int)(2 * kRowSlots / 16); k += R) z4[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+        } else {
+            if (leader) ok = mbar_wait(bar, parity);
+            __syncthreads();
+            if (!ok) {
+                if (leader) mbar_wait(bar, parity);
+                break;
+            }
+            if (!leader) mbar_wait(bar, parity);
+            parity ^= 1u;
+            float2 v[R];
 #pragma unroll
-        for (int j = 0; j < R; ++j)
-            v[j] = (j >= J0 && j < J1) ? make_float2(in_a[t + R * (j - J0)], in_b[t + R * (j - J0)])
-                                       : make_float2(0.0f, 0.0f);
-        if (leader) bulk_wait_read_all();  // the previous pair's spectrum rows have left the area
-        __syncthreads();                   // IN consumed
-        const int pn = p + gridDim.x;
-        if (leader && pn < PAIRS) {
-            fence_proxy_async();
-            mbar_expect_tx(bar, kRowInBytes);
-            bulk_load((void *)in_a, x + (size_t)(2 * pn) * HALF, kRowInBytes, bar);
-        }
-        dft64<false, false>(v);
-        twiddle_t<false, true>(v, t, W4096{});
+            for (int j = 0; j < R; ++j)
+                v[j] = (j >= J0 && j < J1) ? make_float2(in_a[t + R * (j - J0)], in_b[t + R * (j - J0)])
+                                           : make_float2(0.0f, 0.0f);
+            if (leader) bulk_wait_read_all();  // the previous pair's spectrum rows have left the area
+            __syncthreads();                   // IN consumed
+            const int in_next = item + gridDim.x;
+            if (leader && in_next < n_work) {
+                fence_proxy_async();
+                mbar_expect_tx(bar, kRowInBytes);
+                bulk_load((void *)in_a, x + (size_t)(2 * pair_of(in_next)) * HALF, kRowInBytes, bar);
+            }
+            dft64<false, false>(v);
+            twiddle_t<false, true>(v, t, W4096{});
 #pragma unroll
-        for (int k1 = 0; k1 < R; ++k1) buf[k1 * PADR + t] = v[tslot(k1)];
-        __syncthreads();
+            for (int k1 = 0; k1 < R; ++k1) buf[k1 * PADR + t] = v[tslot(k1)];
+            __syncthreads();
 #pragma unroll
-        for (int n1 = 0; n1 < R; ++n1) v[n1] = buf[t * PADR + n1];
-        __syncthreads();
-        dft64<false, false>(v);  // Z[t + 64 k2] in slot tslot(k2)
+            for (int n1 = 0; n1 < R; ++n1) v[n1] = buf[t * PADR + n1];
+            __syncthreads();
+            dft64<false, false>(v);  // Z[t + 64 k2] in slot tslot(k2)
 #pragma unroll
-        for (int k2 = 0; k2 < R; ++k2) {
-            const int k = t + R * k2;
-            const float2 z = v[tslot(k2)];
-            if (k <= HALF) *reinterpret_cast<float2 *>(out_lo + slot_off(k)) = z;
-            if (k >= HALF) *reinterpret_cast<float2 *>(out_hi + slot_off(M - k)) = z;
-            if (k == 0) *reinterpret_cast<float2 *>(out_hi) = z;
+            for (int k2 = 0; k2 < R; ++k2) {
+                const int k = t + R * k2;
+                const float2 z = v[tslot(k2)];
+                if (k <= HALF) *reinterpret_cast<float2 *>(out_lo + slot_off(k)) = z;
+                if (k >= HALF) *reinterpret_cast<float2 *>(out_hi + slot_off(M - k)) = z;
+                if (k == 0) *reinterpret_cast<float2 *>(out_hi) = z;
+            }
         }
         fence_proxy_async();
         __syncthreads();
@@ -721,13 +778,14 @@ inline int launch_config(SqLaunch *cfg) {
     return MSN_OK;
 }
 
-int conv_run(const float *x, const float2 *spec, float *out, float2 *lo, float2 *hi, cudaStream_t st) {
+int conv_run(const float *x, const float2 *spec, float *out, float2 *lo, float2 *hi, cudaStream_t st,
+             const unsigned char *rows) {
     SqLaunch cfg;
     MSN_TRY(launch_config(&cfg));
     CUtensorMap lo_map, hi_map;
     MSN_TRY(plane_map(&lo_map, lo));
     MSN_TRY(plane_map(&hi_map, hi));
-    sq_rows_fwd<<<cfg.fwd_grid, R, kRowFwdSmem, st>>>(x, lo_map, hi_map);
+    sq_rows_fwd<<<cfg.fwd_grid, R, kRowFwdSmem, st>>>(x, lo_map, hi_map, rows);
     MSN_TRY(check_launch("sq_rows_fwd"));
     sq_cols_conv<<<cfg.col_grid, R * TEAMS, kColSmem, st>>>(lo, hi, spec);
     MSN_TRY(check_launch("sq_cols_conv"));

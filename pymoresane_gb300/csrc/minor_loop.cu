@@ -103,13 +103,16 @@ __global__ void minor_control(MinorState *s, const double *snr2, double *hist, i
 // and x = xn when the control kernel kept this iteration's xn.
 // r.r of the next iteration is this iteration's rn.rn (r = rn; same values, same
 // reduction order), so it is carried in the scalar block instead of recomputed.
+// Rows outside the support hold zeros in every vector and are not touched.
 __global__ void direction_commit(const float4 *__restrict__ rn, float4 *__restrict__ p, float4 *__restrict__ r,
                                  const float4 *__restrict__ xn, float4 *__restrict__ x,
-                                 double *__restrict__ scal, const MinorState *__restrict__ s, size_t n4) {
+                                 double *__restrict__ scal, const MinorState *__restrict__ s, size_t n4,
+                                 RowSupport sup) {
     const float b = (float)scal[S_BETA];
     const bool commit = s->commit != 0;
     if (blockIdx.x == 0 && threadIdx.x == 0) scal[S_RR] = scal[S_RNRN];
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n4; i += (size_t)gridDim.x * blockDim.x) {
+        if (!sup.active(i)) continue;
         const float4 rv = __ldg(rn + i);
         float4 pv = p[i];
         pv.x = __fadd_rn(rv.x, __fmul_rn(b, pv.x));
@@ -197,7 +200,10 @@ msn_minor_args make_key(const msn_minor_args *a) {
 // (main.py:375-384).
 int apply_a(const msn_minor_args *a, const float *in, float *out, cudaStream_t st) {
     const int planes = a->max_scale - a->scale_adjust;
-    MSN_TRY(msn_fft_convolve(in, a->n, a->m, a->spec, a->tmp, a->linear, a->fft_work, a->fft_work_bytes, st));
+    // in (p) is zero outside the level-0 support of the recomposition: the convolution skips
+    // the row transforms of pairs of zero rows
+    MSN_TRY(fft_convolve_rows(in, a->n, a->m, a->spec, a->tmp, a->linear, a->fft_work, a->fft_work_bytes,
+                              a->rec_rows, st));
     // rows whose mask row is empty stay zero (cleared in the prologue)
     MSN_TRY(msn_iuwt_decompose_masked_rows(a->tmp, a->emask, a->row_flags, a->planes, a->n, a->n, a->max_scale,
                                            a->scale_adjust, a->iuwt_work, a->iuwt_work_bytes, st));
@@ -273,6 +279,11 @@ int build_graph(Engine *e, const msn_minor_args *a, CacheEntry *ce) {
         // A p and the recomposition planes: rows outside the recomposition's support stay zero
         MSN_TRY(check_cuda(cudaMemsetAsync(a->ap, 0, nvec * sizeof(float), st), "zero Ap"));
         MSN_TRY(check_cuda(cudaMemsetAsync(a->iuwt_work, 0, a->iuwt_work_bytes, st), "zero IUWT workspace"));
+        // x, r, p, A p (and xn, rn) are zero outside the level-0 support of the recomposition
+        // (rec_rows[0 .. n)); the vector passes of the loop body skip those rows, so xn and rn
+        // start at zero there
+        MSN_TRY(check_cuda(cudaMemsetAsync(a->xn, 0, nvec * sizeof(float), st), "zero xn"));
+        MSN_TRY(check_cuda(cudaMemsetAsync(a->rn, 0, nvec * sizeof(float), st), "zero rn"));
         minor_init<<<1, 1, 0, st>>>(state, a->minor_loop_miter);
         MSN_TRY(check_launch("minor_init"));
         return add_conditional(st, while_h, cudaGraphCondTypeWhile, &body);
@@ -282,11 +293,12 @@ int build_graph(Engine *e, const msn_minor_args *a, CacheEntry *ce) {
     if (a->enforce_positivity)
         MSN_TRY(check_cuda(cudaGraphConditionalHandleCreate(&if_h, body, 0u, 0u), "positivity handle"));
     long long branch_kernels = 0;
+    const RowSupport sup{a->rec_rows, (unsigned)(a->n / 4)};
     MSN_TRY(capture_into(e->cs[1], body, &ce->body_kernels, [&](cudaStream_t st) -> int {
         MSN_TRY(apply_a(a, a->p, a->ap, st));
         // p.Ap into scal[S_PAP] (the second output, scal[S_ALPHA], is rewritten right after);
         // r.r is carried from the previous iteration (direction_commit) or the prologue
-        MSN_TRY(msn_dot2(a->p, a->ap, nullptr, nullptr, nvec, a->scal + S_PAP, a->red_work, a->red_work_bytes, st));
+        MSN_TRY(dot_rows(a->p, a->ap, nvec, sup, a->scal + S_PAP, a->red_work, a->red_work_bytes, st));
         if (a->enforce_positivity) {
             MSN_TRY(msn_cg_alpha_x(a->x, a->p, a->scal, a->xn, nvec, a->neg, st));
             positivity_gate<<<1, 1, 0, st>>>(a->neg, state, if_h);
@@ -299,8 +311,8 @@ int build_graph(Engine *e, const msn_minor_args *a, CacheEntry *ce) {
             }));
         } else {
             // xn = x + alpha p and rn = r - alpha Ap (with rn.rn, beta) in one pass
-            MSN_TRY(msn_cg_step(a->x, a->p, a->r, a->ap, a->scal, a->xn, a->rn, nvec, a->red_work,
-                                a->red_work_bytes, st));
+            MSN_TRY(cg_step_rows(a->x, a->p, a->r, a->ap, a->scal, a->xn, a->rn, nvec, sup, a->red_work,
+                                 a->red_work_bytes, st));
         }
         MSN_TRY(msn_snr_update_masked(a->esrc, a->ms, a->planes, a->scal, (size_t)planes * nvec, a->seg_flags,
                                       a->snr2, a->red_work, a->red_work_bytes, st));
@@ -310,7 +322,7 @@ int build_graph(Engine *e, const msn_minor_args *a, CacheEntry *ce) {
             MSN_TRY(msn_cg_residual(a->r, a->ap, a->scal, a->rn, nvec, a->red_work, a->red_work_bytes, st));
         direction_commit<<<ew_grid4(nvec / 4), 256, 0, st>>>(
             (const float4 *)a->rn, (float4 *)a->p, (float4 *)a->r, (const float4 *)a->xn, (float4 *)a->x, a->scal,
-            state, nvec / 4);
+            state, nvec / 4, sup);
         return check_launch("direction_commit");
     }));
     // branch kernels were counted inside the body capture as well

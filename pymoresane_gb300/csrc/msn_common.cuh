@@ -39,6 +39,31 @@ enum Knob {
 int tune_value(Knob k);
 unsigned tune_epoch();
 
+// The rows of a row-major vector [rows][cols] that may hold non-zero values:
+// rows[r] != 0 (null: every row). A pass over the vector skips the float4
+// elements of the other rows, where every operand is zero, so each result it
+// writes or sums is the dense pass's (a skipped term would add an exact zero).
+// cols4 = cols / 4.
+struct RowSupport {
+    const unsigned char *rows;
+    unsigned cols4;
+    __device__ __forceinline__ bool active(size_t i4) const {
+        return !rows || __ldg(rows + (unsigned)i4 / cols4) != 0;
+    }
+};
+
+// msn_fft_convolve with the rows of d_x that may be non-zero (rows[r] != 0, null: every row);
+// the four-step kernels skip the row transforms of pairs of zero rows (fft.cu).
+int fft_convolve_rows(const float *d_x, int n, int m, const void *d_spec, float *d_out, int linear, void *d_work,
+                      size_t work_bytes, const unsigned char *rows, cudaStream_t st);
+
+// cg.cu entry points of the graph minor loop with a row support: out[0] = a . b,
+// and the conjugate-gradient step of msn_cg_step.
+int dot_rows(const float *a, const float *b, size_t n, RowSupport sup, double *out, void *work, size_t work_bytes,
+             cudaStream_t st);
+int cg_step_rows(const float *x, const float *p, const float *r, const float *ap, double *scal, float *xn, float *rn,
+                 size_t n, RowSupport sup, void *work, size_t work_bytes, cudaStream_t st);
+
 inline cudaStream_t as_stream(void *s) { return reinterpret_cast<cudaStream_t>(s); }
 
 inline bool aligned16(const void *p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }

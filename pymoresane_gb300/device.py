@@ -158,8 +158,12 @@ def pack_spectrum(spec):
     return PsfSpectrum(packed, m)
 
 
-def fft_convolve(x, spec, linear=True, out=None, work=None):
-    """Convolution of the n x n image ``x`` with the PSF of ``spec`` (linear: m == 2n, circular: m == n)."""
+def fft_convolve(x, spec, linear=True, out=None, work=None, rows=None):
+    """Convolution of the n x n image ``x`` with the PSF of ``spec`` (linear: m == 2n, circular: m == n).
+
+    ``rows`` (optional, n uint8 on the device): non-zero where row r of ``x`` may be
+    non-zero; rows flagged zero must hold zeros (msn_fft_convolve_rows).
+    """
     x = as_f32_cuda(x)
     spec = pack_spectrum(spec)
     n = x.shape[0]
@@ -169,8 +173,14 @@ def fft_convolve(x, spec, linear=True, out=None, work=None):
         out = torch.empty((n, n), dtype=torch.float32, device=x.device)
     if work is None:
         work = fft_workspace(n, spec.m, x.device)
-    _native.call("msn_fft_convolve", x.data_ptr(), n, spec.m, spec.packed.data_ptr(), out.data_ptr(),
-                 1 if linear else 0, work.data_ptr(), work.numel(), stream_handle())
+    if rows is None:
+        _native.call("msn_fft_convolve", x.data_ptr(), n, spec.m, spec.packed.data_ptr(), out.data_ptr(),
+                     1 if linear else 0, work.data_ptr(), work.numel(), stream_handle())
+    else:
+        if rows.dtype != torch.uint8 or rows.numel() < n or not rows.is_cuda:
+            raise ValueError("fft_convolve: rows must be n uint8 flags on the device")
+        _native.call("msn_fft_convolve_rows", x.data_ptr(), n, spec.m, spec.packed.data_ptr(), out.data_ptr(),
+                     1 if linear else 0, rows.data_ptr(), work.data_ptr(), work.numel(), stream_handle())
     return out
 
 

@@ -158,3 +158,35 @@ def test_unaligned_pointers_take_the_stockham_path(cuda):
                  work.data_ptr(), work.numel(), dev.stream_handle())
     got = ou.reshape(2048, 2048)
     assert torch.max(torch.abs(got - ref)).item() <= 1e-5 * torch.max(torch.abs(ref)).item()
+
+
+@pytest.mark.parametrize("n", [2048, 512])
+def test_row_flags_give_the_dense_result(cuda, n):
+    # an image that is zero outside bands of rows, convolved with the flags of its possibly
+    # non-zero rows: the same result as the dense convolution (the 2048^2 linear case skips the
+    # row transforms of pairs of zero rows; other sizes ignore the flags). Flag patterns: bands
+    # with odd edges (pairs with one live row), everything, nothing, a single row
+    rng = np.random.default_rng(n)
+    spec = dev.psf_spectrum(make_psf(2 * n, 2000, rng))
+    patterns = []
+    rows = np.zeros(n, np.uint8)
+    rows[n // 16 + 1:n // 8] = 1
+    rows[n // 2:n // 2 + n // 5 + 1] = 1
+    rows[n - 3:] = 1
+    patterns.append(rows)
+    patterns.append(np.ones(n, np.uint8))
+    patterns.append(np.zeros(n, np.uint8))
+    one = np.zeros(n, np.uint8)
+    one[n // 3] = 1
+    patterns.append(one)
+    work = dev.fft_workspace(n, 2 * n, torch.device("cuda"))
+    for flags in patterns:
+        x = rng.standard_normal((n, n)).astype(np.float32) * flags[:, None].astype(np.float32)
+        xd = torch.from_numpy(x).cuda()
+        dense = dev.fft_convolve(xd, spec, work=work).clone()
+        # stale values in the workspace must not leak into skipped rows
+        work.fill_(7)
+        got = dev.fft_convolve(xd, spec, work=work, rows=torch.from_numpy(flags).cuda())
+        assert torch.equal(got, dense), int(flags.sum())
+    with pytest.raises(ValueError):
+        dev.fft_convolve(xd, spec, rows=torch.zeros(n, dtype=torch.int32, device="cuda"))
