@@ -11,6 +11,7 @@
 // alpha and beta on the device and the host only needs the stop decisions.
 #include <atomic>
 
+#include "minor_state.cuh"
 #include "msn_common.cuh"
 
 namespace msn {
@@ -399,6 +400,80 @@ cg_step(const float4 *__restrict__ x, const float4 *__restrict__ p, const float4
     finish_pairs<T>(s, T(0), partials, scal + S_RNRN, scal, 1, 0);
 }
 
+// The graph minor loop's pass after p.Ap without positivity, in one launch: cg_step
+// on the row support (xn, rn, rn.rn, beta), then snr_update's model-source update
+// and SNR sums (same alpha: the same float64 quotient rounded to float32), then, in
+// the CTA that completes the SNR sums, the stop rules (minor_control_apply). Each
+// sum keeps its kernel's grid, per-thread order and cross-CTA order, in its own
+// set of partials, so every result is bit-identical to the three launches.
+template <class T>
+__global__ void __launch_bounds__(kRedThreads)
+cg_step_snr(const float4 *__restrict__ x, const float4 *__restrict__ p, const float4 *__restrict__ r,
+            const float4 *__restrict__ ap, double *__restrict__ scal, float4 *__restrict__ xn,
+            float4 *__restrict__ rn, size_t n4, RowSupport sup, const float4 *__restrict__ e,
+            float4 *__restrict__ ms, const float4 *__restrict__ q, size_t nq4,
+            const unsigned char *__restrict__ seg_flags, double *__restrict__ partials_rn,
+            double *__restrict__ partials_snr, double *__restrict__ snr2, MinorState *state, double *hist,
+            int hist_len, cudaGraphConditionalHandle h) {
+    const double alpha = scal[S_RR] / scal[S_PAP];
+    if (blockIdx.x == 0 && threadIdx.x == 0) scal[S_ALPHA] = alpha;
+    const float a = (float)alpha;
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    // the CG step (cg_step)
+    T s = T(0);
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n4; i += stride) {
+        if (!sup.active(i)) continue;
+        const float4 xv = __ldg(x + i), pv = __ldg(p + i), rv = __ldg(r + i), av = __ldg(ap + i);
+        float4 v, u;
+        v.x = __fadd_rn(xv.x, __fmul_rn(a, pv.x));
+        v.y = __fadd_rn(xv.y, __fmul_rn(a, pv.y));
+        v.z = __fadd_rn(xv.z, __fmul_rn(a, pv.z));
+        v.w = __fadd_rn(xv.w, __fmul_rn(a, pv.w));
+        xn[i] = v;
+        u.x = __fsub_rn(rv.x, __fmul_rn(a, av.x));
+        u.y = __fsub_rn(rv.y, __fmul_rn(a, av.y));
+        u.z = __fsub_rn(rv.z, __fmul_rn(a, av.z));
+        u.w = __fsub_rn(rv.w, __fmul_rn(a, av.w));
+        rn[i] = u;
+        s += (T)dot4(u, u);
+    }
+    // the model sources and SNR sums (snr_update)
+    T s0 = T(0), s1 = T(0);
+    int worked = 0;
+    constexpr int kAhead = 8;
+    for (size_t i0 = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i0 < nq4; i0 += kAhead * stride) {
+        unsigned char f[kAhead];
+#pragma unroll
+        for (int u = 0; u < kAhead; ++u) {
+            const size_t i = i0 + u * stride;
+            f[u] = i < nq4 ? __ldg(seg_flags + (i >> 5)) : (unsigned char)0;
+        }
+#pragma unroll
+        for (int u = 0; u < kAhead; ++u) {
+            if (!f[u]) continue;
+            const size_t i = i0 + u * stride;
+            worked = 1;
+            const float4 ev = __ldg(e + i), qv = __ldg(q + i);
+            float4 mv = ms[i];
+            mv.x = __fadd_rn(mv.x, __fmul_rn(a, qv.x));
+            mv.y = __fadd_rn(mv.y, __fmul_rn(a, qv.y));
+            mv.z = __fadd_rn(mv.z, __fmul_rn(a, qv.z));
+            mv.w = __fadd_rn(mv.w, __fmul_rn(a, qv.w));
+            ms[i] = mv;
+            s0 += (T)dot4(ev, ev);
+            s1 += (T)sqdiff4(ev, mv);
+        }
+    }
+    // scal[S_RNRN] = rn.rn, scal[S_BETA] = rn.rn / r.r
+    finish_pairs<T>(s, T(0), partials_rn, scal + S_RNRN, scal, 1, 0);
+    __syncthreads();  // finish_pairs' shared state is reused below
+    const int any = __syncthreads_or(worked);
+    if (finish_pairs<T>(s0, s1, partials_snr, snr2, nullptr, any) && threadIdx.x == 0) {
+        __threadfence();
+        minor_control_apply(state, snr2, hist, hist_len, h);
+    }
+}
+
 // flags[s] = 1 when any element of float4 segment s (32 float4) of m is non-zero.
 __global__ void segment_flags(const float4 *__restrict__ m, size_t n4, unsigned char *__restrict__ flags) {
     const size_t nseg = (n4 + 31) / 32;
@@ -545,7 +620,10 @@ int ew_grid(size_t n) {
 
 // kRedGrid partial pairs and the completion counter of finish_pairs (zero
 // between calls: the workspace is zeroed once when it is allocated).
-constexpr size_t kPartialBytes = 2 * kRedGrid * sizeof(double) + 16;
+// One set of partials: kRedGrid pairs and the completion counter. The workspace holds two
+// sets (the fused CG / SNR pass runs two reductions at once).
+constexpr size_t kPartialSetBytes = 2 * kRedGrid * sizeof(double) + 16;
+constexpr size_t kPartialBytes = 2 * kPartialSetBytes;
 
 }  // namespace
 
@@ -575,6 +653,24 @@ int dot_rows(const float *a, const float *b, size_t n, RowSupport sup, double *o
     if (!a || !b || !out || !work || work_bytes < kPartialBytes || !sup.rows || sup.cols4 == 0)
         return set_error(MSN_ERR_INVALID, "dot_rows: bad arguments");
     return dual_reduce(a, b, nullptr, nullptr, n, false, out, (double *)work, st, sup);
+}
+
+int cg_step_snr_rows(const float *x, const float *p, const float *r, const float *ap, double *scal, float *xn,
+                     float *rn, size_t n, RowSupport sup, const float *e, float *ms, const float *q, size_t nq,
+                     const unsigned char *seg_flags, double *snr2, MinorState *state, double *hist, int hist_len,
+                     cudaGraphConditionalHandle h, void *work, size_t work_bytes, cudaStream_t st) {
+    if (!x || !p || !r || !ap || !scal || !xn || !rn || !e || !ms || !q || !seg_flags || !snr2 || !state || !hist ||
+        !work || work_bytes < kPartialBytes || sup.cols4 == 0)
+        return set_error(MSN_ERR_INVALID, "cg_step_snr_rows: bad arguments");
+    if (n % 4 || nq % 4 || !aligned16(x) || !aligned16(p) || !aligned16(r) || !aligned16(ap) || !aligned16(xn) ||
+        !aligned16(rn) || !aligned16(e) || !aligned16(ms) || !aligned16(q))
+        return set_error(MSN_ERR_INVALID, "cg_step_snr_rows: lengths must be multiples of 4, pointers 16-byte aligned");
+    double *set0 = (double *)work;
+    double *set1 = (double *)((char *)work + kPartialSetBytes);
+    MSN_RED_LAUNCH(cg_step_snr, kRedGrid, kRedThreads, st, (const float4 *)x, (const float4 *)p, (const float4 *)r,
+                   (const float4 *)ap, scal, (float4 *)xn, (float4 *)rn, n / 4, sup, (const float4 *)e, (float4 *)ms,
+                   (const float4 *)q, nq / 4, seg_flags, set0, set1, snr2, state, hist, hist_len, h);
+    return check_launch("cg_step_snr");
 }
 
 int cg_step_rows(const float *x, const float *p, const float *r, const float *ap, double *scal, float *xn, float *rn,

@@ -28,6 +28,7 @@
 #include <mutex>
 #include <vector>
 
+#include "minor_state.cuh"
 #include "msn_common.cuh"
 
 namespace msn {
@@ -38,17 +39,6 @@ void adjust_launches(long long delta);
 namespace {
 
 enum { S_RR = 0, S_PAP = 1, S_ALPHA = 2, S_RNRN = 3, S_BETA = 4 };
-
-struct MinorState {
-    int minor;            // iterations performed
-    int outcome;          // MSN_MINOR_*
-    int commit;           // 1: the iteration's xn becomes x
-    int miter;            // minor_loop_miter
-    int positivity_runs;  // iterations that took the positivity branch
-    int pad;
-    double snr_current;
-    double snr_last;
-};
 
 __global__ void minor_init(MinorState *s, int miter) {
     s->minor = 0;
@@ -68,35 +58,10 @@ __global__ void positivity_gate(const int *neg, MinorState *s, cudaGraphConditio
     cudaGraphSetConditional(h, run ? 1u : 0u);
 }
 
-// SNR and the stop rules of main.py:413-455, in the reference's order:
-//   minor == 1 and SNR > 40  -> false detection (xn discarded)
-//   SNR > 40                 -> converged (xn kept)
-//   minor > 2, SNR <= last   -> stalled (xn discarded)
-//   minor == minor_loop_miter -> iteration cap (xn kept, loop condition ends)
+// SNR and the stop rules (minor_control_apply, minor_state.cuh).
 __global__ void minor_control(MinorState *s, const double *snr2, double *hist, int hist_len,
                               cudaGraphConditionalHandle h) {
-    const double last = s->snr_current;
-    const double cur = 20.0 * log10(sqrt(snr2[0]) / sqrt(snr2[1]));
-    const int minor = s->minor + 1;
-    int outcome = MSN_MINOR_RUNNING, commit = 1;
-    if (minor == 1 && cur > 40.0) {
-        outcome = MSN_MINOR_FALSE_DETECTION;
-        commit = 0;
-    } else if (cur > 40.0) {
-        outcome = MSN_MINOR_CONVERGED;
-    } else if (minor > 2 && cur <= last) {
-        outcome = MSN_MINOR_STALLED;
-        commit = 0;
-    } else if (minor >= s->miter) {
-        outcome = MSN_MINOR_ITERATION_CAP;
-    }
-    s->snr_last = last;
-    s->snr_current = cur;
-    s->minor = minor;
-    s->outcome = outcome;
-    s->commit = commit;
-    if (minor - 1 < hist_len) hist[minor - 1] = cur;
-    cudaGraphSetConditional(h, outcome == MSN_MINOR_RUNNING ? 1u : 0u);
+    minor_control_apply(s, snr2, hist, hist_len, h);
 }
 
 // p = rn + beta p (main.py:411, the arithmetic of msn_cg_direction), r = rn,
@@ -309,17 +274,18 @@ int build_graph(Engine *e, const msn_minor_args *a, CacheEntry *ce) {
                 MSN_TRY(msn_cg_positivity(a->x, a->xn, a->p, a->scal, nvec, bst));
                 return apply_a(a, a->p, a->ap, bst);
             }));
-        } else {
-            // xn = x + alpha p and rn = r - alpha Ap (with rn.rn, beta) in one pass
-            MSN_TRY(cg_step_rows(a->x, a->p, a->r, a->ap, a->scal, a->xn, a->rn, nvec, sup, a->red_work,
-                                 a->red_work_bytes, st));
-        }
-        MSN_TRY(msn_snr_update_masked(a->esrc, a->ms, a->planes, a->scal, (size_t)planes * nvec, a->seg_flags,
-                                      a->snr2, a->red_work, a->red_work_bytes, st));
-        minor_control<<<1, 1, 0, st>>>(state, a->snr2, hist, kHistory, while_h);
-        MSN_TRY(check_launch("minor_control"));
-        if (a->enforce_positivity)
+            MSN_TRY(msn_snr_update_masked(a->esrc, a->ms, a->planes, a->scal, (size_t)planes * nvec, a->seg_flags,
+                                          a->snr2, a->red_work, a->red_work_bytes, st));
+            minor_control<<<1, 1, 0, st>>>(state, a->snr2, hist, kHistory, while_h);
+            MSN_TRY(check_launch("minor_control"));
             MSN_TRY(msn_cg_residual(a->r, a->ap, a->scal, a->rn, nvec, a->red_work, a->red_work_bytes, st));
+        } else {
+            // xn = x + alpha p and rn = r - alpha Ap (with rn.rn, beta), MS += alpha Q with the SNR
+            // sums, and the stop rules: one launch
+            MSN_TRY(cg_step_snr_rows(a->x, a->p, a->r, a->ap, a->scal, a->xn, a->rn, nvec, sup, a->esrc, a->ms,
+                                     a->planes, (size_t)planes * nvec, a->seg_flags, a->snr2, state, hist, kHistory,
+                                     while_h, a->red_work, a->red_work_bytes, st));
+        }
         direction_commit<<<ew_grid4(nvec / 4), 256, 0, st>>>(
             (const float4 *)a->rn, (float4 *)a->p, (float4 *)a->r, (const float4 *)a->xn, (float4 *)a->x, a->scal,
             state, nvec / 4, sup);
