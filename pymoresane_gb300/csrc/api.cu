@@ -34,6 +34,11 @@ void count_launch() {
     ++t_launches;
 }
 
+bool &pdl_flag() {
+    static thread_local bool flag = false;
+    return flag;
+}
+
 // Launches issued by the calling thread (graph capture measures its own).
 unsigned long long thread_launches() { return t_launches; }
 

@@ -165,6 +165,8 @@ __global__ void __launch_bounds__(kRedThreads)
 dual_partials(const float4 *__restrict__ a, const float4 *__restrict__ b, const float4 *__restrict__ c,
               const float4 *__restrict__ d, size_t n4, double *__restrict__ partials, double *__restrict__ out,
               RowSupport sup) {
+    pdl_wait();
+    pdl_trigger();
     T s0 = T(0), s1 = T(0);
     const size_t stride = (size_t)gridDim.x * blockDim.x;
     size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -415,6 +417,8 @@ cg_step_snr(const float4 *__restrict__ x, const float4 *__restrict__ p, const fl
             const unsigned char *__restrict__ seg_flags, double *__restrict__ partials_rn,
             double *__restrict__ partials_snr, double *__restrict__ snr2, MinorState *state, double *hist,
             int hist_len, cudaGraphConditionalHandle h) {
+    pdl_wait();
+    pdl_trigger();
     const double alpha = scal[S_RR] / scal[S_PAP];
     if (blockIdx.x == 0 && threadIdx.x == 0) scal[S_ALPHA] = alpha;
     const float a = (float)alpha;
@@ -633,19 +637,16 @@ int dual_reduce(const float *a, const float *b, const float *c, const float *d, 
         return set_error(MSN_ERR_INVALID, "reduction: length must be a multiple of 4 and pointers 16-byte aligned");
     const float4 *a4 = (const float4 *)a, *b4 = (const float4 *)b, *c4 = (const float4 *)c, *d4 = (const float4 *)d;
     const int bits = g_reduce_bits.load(std::memory_order_relaxed);
-    if (diff && bits == 32)
-        dual_partials<true, float><<<kRedGrid, kRedThreads, 0, st>>>(a4, b4, c4, d4, n / 4, partials, out, sup);
-    else if (diff && bits == 64)
-        dual_partials<true, double><<<kRedGrid, kRedThreads, 0, st>>>(a4, b4, c4, d4, n / 4, partials, out, sup);
-    else if (diff)
-        dual_partials<true, FF><<<kRedGrid, kRedThreads, 0, st>>>(a4, b4, c4, d4, n / 4, partials, out, sup);
-    else if (bits == 32)
-        dual_partials<false, float><<<kRedGrid, kRedThreads, 0, st>>>(a4, b4, c4, d4, n / 4, partials, out, sup);
-    else if (bits == 64)
-        dual_partials<false, double><<<kRedGrid, kRedThreads, 0, st>>>(a4, b4, c4, d4, n / 4, partials, out, sup);
-    else
-        dual_partials<false, FF><<<kRedGrid, kRedThreads, 0, st>>>(a4, b4, c4, d4, n / 4, partials, out, sup);
-    return check_launch("dual_partials");
+    auto go = [&](auto kernel) {
+        return launch_k("dual_partials", kernel, kRedGrid, kRedThreads, 0, st, a4, b4, c4, d4, n / 4, partials, out, sup);
+    };
+    if (diff && bits == 32) return go(dual_partials<true, float>);
+    if (diff && bits == 64) return go(dual_partials<true, double>);
+    if (diff) return go(dual_partials<true, FF>);
+    if (bits == 32) return go(dual_partials<false, float>);
+    if (bits == 64) return go(dual_partials<false, double>);
+    return go(dual_partials<false, FF>);
+
 }
 
 int dot_rows(const float *a, const float *b, size_t n, RowSupport sup, double *out, void *work, size_t work_bytes,
@@ -667,10 +668,16 @@ int cg_step_snr_rows(const float *x, const float *p, const float *r, const float
         return set_error(MSN_ERR_INVALID, "cg_step_snr_rows: lengths must be multiples of 4, pointers 16-byte aligned");
     double *set0 = (double *)work;
     double *set1 = (double *)((char *)work + kPartialSetBytes);
-    MSN_RED_LAUNCH(cg_step_snr, kRedGrid, kRedThreads, st, (const float4 *)x, (const float4 *)p, (const float4 *)r,
-                   (const float4 *)ap, scal, (float4 *)xn, (float4 *)rn, n / 4, sup, (const float4 *)e, (float4 *)ms,
-                   (const float4 *)q, nq / 4, seg_flags, set0, set1, snr2, state, hist, hist_len, h);
-    return check_launch("cg_step_snr");
+    auto go = [&](auto kernel) {
+        return launch_k("cg_step_snr", kernel, kRedGrid, kRedThreads, 0, st, (const float4 *)x, (const float4 *)p,
+                        (const float4 *)r, (const float4 *)ap, scal, (float4 *)xn, (float4 *)rn, n / 4, sup,
+                        (const float4 *)e, (float4 *)ms, (const float4 *)q, nq / 4, seg_flags, set0, set1, snr2, state,
+                        hist, hist_len, h);
+    };
+    const int bits = g_reduce_bits.load(std::memory_order_relaxed);
+    if (bits == 32) return go(cg_step_snr<float>);
+    if (bits == 64) return go(cg_step_snr<double>);
+    return go(cg_step_snr<FF>);
 }
 
 int cg_step_rows(const float *x, const float *p, const float *r, const float *ap, double *scal, float *xn, float *rn,

@@ -353,6 +353,8 @@ static_assert(kPairsPerThread * R == PAIRS && kPairsPerThread <= 32, "work-list 
 __global__ void __launch_bounds__(R, 4)
 sq_rows_fwd(const float *__restrict__ x, const __grid_constant__ CUtensorMap lo_map,
             const __grid_constant__ CUtensorMap hi_map, const unsigned char *__restrict__ rows) {
+    pdl_wait();
+    pdl_trigger();
     extern __shared__ __align__(128) float2 smem[];
     const int t = threadIdx.x;
     const bool leader = t == 0;
@@ -493,6 +495,8 @@ static_assert(4 * kBlockBytes <= kAreaBytes, "IN and OUT must fit in the exchang
 
 __global__ void __launch_bounds__(R * TEAMS, 3)
 sq_cols_conv(float2 *lo, float2 *hi, const float2 *__restrict__ h) {
+    pdl_wait();
+    pdl_trigger();
     extern __shared__ __align__(128) float2 smem[];
     constexpr int G = (W + 1) / 2;
     constexpr unsigned kHBytes = M * 2 * sizeof(float2);  // a group's PSF-spectrum block, 64 KB
@@ -653,6 +657,8 @@ static_assert(2 * kRowSlots <= kTeamArea, "a pair's lo and hi rows fit in the ex
 __global__ void __launch_bounds__(R, 4)
 sq_rows_inv(const __grid_constant__ CUtensorMap lo_map, const __grid_constant__ CUtensorMap hi_map,
             float *__restrict__ out) {
+    pdl_wait();
+    pdl_trigger();
     extern __shared__ __align__(128) float2 smem[];
     const int t = threadIdx.x;
     const bool leader = t == 0;
@@ -785,12 +791,9 @@ int conv_run(const float *x, const float2 *spec, float *out, float2 *lo, float2 
     CUtensorMap lo_map, hi_map;
     MSN_TRY(plane_map(&lo_map, lo));
     MSN_TRY(plane_map(&hi_map, hi));
-    sq_rows_fwd<<<cfg.fwd_grid, R, kRowFwdSmem, st>>>(x, lo_map, hi_map, rows);
-    MSN_TRY(check_launch("sq_rows_fwd"));
-    sq_cols_conv<<<cfg.col_grid, R * TEAMS, kColSmem, st>>>(lo, hi, spec);
-    MSN_TRY(check_launch("sq_cols_conv"));
-    sq_rows_inv<<<cfg.inv_grid, R, kRowInvSmem, st>>>(lo_map, hi_map, out);
-    return check_launch("sq_rows_inv");
+    MSN_TRY(launch_k("sq_rows_fwd", sq_rows_fwd, cfg.fwd_grid, R, kRowFwdSmem, st, x, lo_map, hi_map, rows));
+    MSN_TRY(launch_k("sq_cols_conv", sq_cols_conv, cfg.col_grid, R * TEAMS, kColSmem, st, lo, hi, spec));
+    return launch_k("sq_rows_inv", sq_rows_inv, cfg.inv_grid, R, kRowInvSmem, st, lo_map, hi_map, out);
 }
 
 #endif  // MSN_SQ_KERNELS

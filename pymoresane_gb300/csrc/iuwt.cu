@@ -89,6 +89,8 @@ atrous_band(const float *__restrict__ in, float *__restrict__ out, const float *
             const float *__restrict__ mask, int ny, int nx, int d, int band_rows,
             const unsigned char *__restrict__ row_flags, int skip_inactive,
             const unsigned char *__restrict__ zero_rows) {
+    pdl_wait();
+    pdl_trigger();
     extern __shared__ float4 smem4[];
     // masked detail with row flags: rows whose mask row is empty are left as they are (zero)
     if (EPI == kDetailMask && row_flags && band_rows == 1 && !row_flags[blockIdx.x]) return;
@@ -173,6 +175,8 @@ template <bool MASK>
 __global__ void __launch_bounds__(kThreads)
 atrous_pair(const float *__restrict__ in, const float *c0, const float *__restrict__ mask, float *__restrict__ w,
             float *next, int ny, int nx, int d, const unsigned char *__restrict__ row_flags) {
+    pdl_wait();
+    pdl_trigger();
     extern __shared__ float4 smem4[];
     const int r = blockIdx.x;
     // with row flags, a row whose mask row is empty only needs the next smoothing
@@ -252,6 +256,8 @@ __global__ void recompose_activity(const unsigned char *__restrict__ qrows, int 
 // (the smoothing of an all-zero plane is exactly +0, and +0 + w maps -0 to +0
 // exactly as the reference's addition does).
 __global__ void zero_plus(const float4 *__restrict__ w, float4 *__restrict__ out, size_t n4) {
+    pdl_wait();
+    pdl_trigger();
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n4; i += (size_t)gridDim.x * blockDim.x) {
         float4 v = __ldg(w + i);
         v.x = __fadd_rn(0.0f, v.x);
@@ -266,6 +272,8 @@ __global__ void zero_plus(const float4 *__restrict__ w, float4 *__restrict__ out
 // not touched (the caller keeps them at zero).
 __global__ void zero_plus_rows(const float4 *__restrict__ w, float4 *__restrict__ out, int nx4,
                                const unsigned char *__restrict__ act, const unsigned char *__restrict__ zero_rows) {
+    pdl_wait();
+    pdl_trigger();
     const size_t base = (size_t)blockIdx.x * nx4;
     if (!act[blockIdx.x]) {
         if (zero_rows && zero_rows[blockIdx.x])
@@ -303,9 +311,8 @@ int launch_band(const float *in, float *out, const float *aux, int ny, int nx, i
     const int work4 = band * (nx >> 2);
     const int cta = tune_value(nx <= 2048 ? kKnobIuwtThreads : kKnobIuwtThreadsWide);  // 64, 128 or 256
     const int threads = work4 >= cta ? cta : ((work4 + 31) / 32) * 32;
-    atrous_band<EPI><<<grid, threads, smem, st>>>(in, out, aux, mask, ny, nx, d, band, row_flags, skip_inactive,
-                                                   zero_rows);
-    return check_launch("atrous_band");
+    return launch_k("atrous_band", atrous_band<EPI>, grid, threads, smem, st, in, out, aux, mask, ny, nx, d, band,
+                    row_flags, skip_inactive, zero_rows);
 }
 
 // The fused step keeps two rows in shared memory.
@@ -321,17 +328,16 @@ int launch_pair(const float *in, const float *c0, const float *mask, float *w, f
     const int nx4 = nx >> 2;
     const int cta = tune_value(nx <= 2048 ? kKnobIuwtThreads : kKnobIuwtThreadsWide);  // 64, 128 or 256
     const int threads = nx4 >= cta ? cta : ((nx4 + 31) / 32) * 32;
-    atrous_pair<MASK><<<ny, threads, 2 * (size_t)nx * sizeof(float), st>>>(in, c0, mask, w, next, ny, nx, d,
-                                                                            row_flags);
-    return check_launch("atrous_pair");
+    return launch_k("atrous_pair", atrous_pair<MASK>, ny, threads, 2 * (size_t)nx * sizeof(float), st, in, c0, mask, w,
+                    next, ny, nx, d, row_flags);
 }
 
 int launch_zero_plus(const float *w, float *out, size_t n, cudaStream_t st) {
     const size_t n4 = n / 4;
     int grid = (int)((n4 + kThreads - 1) / kThreads);
     if (grid > 152 * 16) grid = 152 * 16;
-    zero_plus<<<grid, kThreads, 0, st>>>(reinterpret_cast<const float4 *>(w), reinterpret_cast<float4 *>(out), n4);
-    return check_launch("zero_plus");
+    return launch_k("zero_plus", zero_plus, grid, kThreads, 0, st, reinterpret_cast<const float4 *>(w),
+                    reinterpret_cast<float4 *>(out), n4);
 }
 
 size_t plane_stride_bytes(int ny, int nx) { return (((size_t)ny * nx * sizeof(float)) + 255) & ~(size_t)255; }
@@ -495,9 +501,8 @@ int iuwt_recompose_impl(const float *d_detail, int planes, const float *d_smooth
         float *dst = dst_for(nb);
         const float *w = d_detail + (size_t)(s - scale_adjust) * plane;
         if (cur == nullptr && skip_inactive) {
-            zero_plus_rows<<<ny, 128, 0, st>>>(reinterpret_cast<const float4 *>(w), reinterpret_cast<float4 *>(dst),
-                                               nx / 4, d_act + (size_t)s * ny, zero_rows_for(dst, nb));
-            MSN_TRY(check_launch("zero_plus_rows"));
+            MSN_TRY(launch_k("zero_plus_rows", zero_plus_rows, ny, 128, 0, st, reinterpret_cast<const float4 *>(w),
+                             reinterpret_cast<float4 *>(dst), nx / 4, d_act + (size_t)s * ny, zero_rows_for(dst, nb)));
         } else if (cur == nullptr) {
             MSN_TRY(launch_zero_plus(w, dst, plane, st));
         } else {

@@ -73,6 +73,8 @@ __global__ void direction_commit(const float4 *__restrict__ rn, float4 *__restri
                                  const float4 *__restrict__ xn, float4 *__restrict__ x,
                                  double *__restrict__ scal, const MinorState *__restrict__ s, size_t n4,
                                  RowSupport sup) {
+    pdl_wait();
+    pdl_trigger();
     const float b = (float)scal[S_BETA];
     const bool commit = s->commit != 0;
     if (blockIdx.x == 0 && threadIdx.x == 0) scal[S_RR] = scal[S_RNRN];
@@ -260,6 +262,8 @@ int build_graph(Engine *e, const msn_minor_args *a, CacheEntry *ce) {
     long long branch_kernels = 0;
     const RowSupport sup{a->rec_rows, (unsigned)(a->n / 4)};
     MSN_TRY(capture_into(e->cs[1], body, &ce->body_kernels, [&](cudaStream_t st) -> int {
+        // the body's kernels may each launch while their predecessor finishes (launch_k)
+        const PdlScope pdl(tune_value(kKnobGraphPdl) != 0);
         MSN_TRY(apply_a(a, a->p, a->ap, st));
         // p.Ap into scal[S_PAP] (the second output, scal[S_ALPHA], is rewritten right after);
         // r.r is carried from the previous iteration (direction_commit) or the prologue
@@ -286,10 +290,9 @@ int build_graph(Engine *e, const msn_minor_args *a, CacheEntry *ce) {
                                      a->planes, (size_t)planes * nvec, a->seg_flags, a->snr2, state, hist, kHistory,
                                      while_h, a->red_work, a->red_work_bytes, st));
         }
-        direction_commit<<<ew_grid4(nvec / 4), 256, 0, st>>>(
-            (const float4 *)a->rn, (float4 *)a->p, (float4 *)a->r, (const float4 *)a->xn, (float4 *)a->x, a->scal,
-            state, nvec / 4, sup);
-        return check_launch("direction_commit");
+        return launch_k("direction_commit", direction_commit, ew_grid4(nvec / 4), 256, 0, st, (const float4 *)a->rn,
+                        (float4 *)a->p, (float4 *)a->r, (const float4 *)a->xn, (float4 *)a->x, a->scal, state,
+                        nvec / 4, sup);
     }));
     // branch kernels were counted inside the body capture as well
     ce->body_kernels -= branch_kernels;

@@ -25,6 +25,43 @@ inline int check_launch(const char *what) {
     return check_cuda(cudaGetLastError(), what);
 }
 
+// Programmatic dependent launch (off by default: tuning value graph_pdl; measured
+// slower on GB300). While the graph minor loop captures its body with it enabled,
+// pdl_flag() is set and the kernels launched with launch_k carry the
+// programmatic-serialization attribute: each may be launched while its
+// predecessor finishes. Every kernel launched through launch_k starts with
+// pdl_wait(), which returns once the predecessor grid has completed and its
+// writes are visible (at once for a kernel launched without the attribute),
+// then pdl_trigger(), which lets its own successor be launched.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;\n" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory"); }
+bool &pdl_flag();  // per host thread (api.cu)
+
+struct PdlScope {
+    bool old;
+    explicit PdlScope(bool on) : old(pdl_flag()) { pdl_flag() = on; }
+    ~PdlScope() { pdl_flag() = old; }
+};
+
+template <class... KArgs, class... Args>
+int launch_k(const char *what, void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st,
+             Args &&...args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    if (pdl_flag()) {
+        attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        attr[0].val.programmaticStreamSerializationAllowed = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+    }
+    count_launch();
+    return check_cuda(cudaLaunchKernelEx(&cfg, kernel, static_cast<Args &&>(args)...), what);
+}
+
 // Tunable launch parameters (tune.cu): the current value of a knob, and an
 // epoch that changes whenever any knob does.
 enum Knob {
@@ -34,6 +71,7 @@ enum Knob {
     kKnobSqInvCtas,
     kKnobIuwtThreads,      // a trous CTA size for rows of up to 2048 floats
     kKnobIuwtThreadsWide,  // ... for wider rows
+    kKnobGraphPdl,         // programmatic dependent launch inside the minor-loop graph
     kKnobCount
 };
 int tune_value(Knob k);

@@ -27,9 +27,11 @@ constexpr KnobSpec kSpecs[kKnobCount] = {
     {"fft_sq_inv_ctas", 0, 0, 8, 0},   // ... of the four-step inverse row kernel
     {"iuwt_threads", 256, 64, 256, 1},      // threads per CTA of the a trous passes, rows of <= 2048 floats
     {"iuwt_threads_wide", 256, 64, 256, 1}, // ... rows of more than 2048 floats
+    {"graph_pdl", 0, 0, 1, 0},         // programmatic dependent launch between the minor-loop graph's kernels
+                                       // (measured slower on GB300: 600 against 516 ms per 2048^2 deconvolution)
 };
 
-std::atomic<int> g_values[kKnobCount] = {{1}, {0}, {0}, {0}, {256}, {256}};
+std::atomic<int> g_values[kKnobCount] = {{1}, {0}, {0}, {0}, {256}, {256}, {0}};
 std::atomic<unsigned> g_epoch{0};
 
 int find(const char *name) {
