@@ -241,20 +241,36 @@ __global__ void decode_max(const int *__restrict__ m, float *__restrict__ out, i
     if (p < planes) out[p] = dec_ord(m[p]);
 }
 
+// seg (may be null): per plane, one byte per 128-float segment (32 float4, the
+// float4 indices of one warp), 1 when the segment holds a non-zero value.
 __global__ void __launch_bounds__(256)
-plane_max_kernel(const float *__restrict__ w, size_t per_plane4, int use_abs, int *__restrict__ plane_max) {
+plane_max_kernel(const float *__restrict__ w, size_t per_plane4, int use_abs, int *__restrict__ plane_max,
+                 unsigned char *__restrict__ seg) {
     const int plane = blockIdx.y;
     const float4 *w4 = reinterpret_cast<const float4 *>(w) + (size_t)plane * per_plane4;
+    unsigned char *seg_p = seg ? seg + (size_t)plane * ((per_plane4 + 31) / 32) : nullptr;
     float mx = -FLT_MAX;
-    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < per_plane4; i += (size_t)gridDim.x * blockDim.x) {
-        float4 v = __ldg(w4 + i);
-        if (use_abs) {
-            v.x = fabsf(v.x);
-            v.y = fabsf(v.y);
-            v.z = fabsf(v.z);
-            v.w = fabsf(v.w);
+    const int lane = threadIdx.x & 31;
+    // warp-aligned bases: the 32 lanes of a warp read one segment
+    for (size_t base = (size_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < per_plane4;
+         base += (size_t)gridDim.x * blockDim.x) {
+        const size_t i = base + lane;
+        bool nz = false;
+        if (i < per_plane4) {
+            float4 v = __ldg(w4 + i);
+            nz = v.x != 0.0f || v.y != 0.0f || v.z != 0.0f || v.w != 0.0f;
+            if (use_abs) {
+                v.x = fabsf(v.x);
+                v.y = fabsf(v.y);
+                v.z = fabsf(v.z);
+                v.w = fabsf(v.w);
+            }
+            mx = fmaxf(mx, fmaxf(fmaxf(v.x, v.y), fmaxf(v.z, v.w)));
         }
-        mx = fmaxf(mx, fmaxf(fmaxf(v.x, v.y), fmaxf(v.z, v.w)));
+        if (seg_p) {
+            const unsigned any = __any_sync(0xffffffffu, nz);
+            if (lane == 0) seg_p[base >> 5] = any ? 1 : 0;
+        }
     }
     for (int off = 16; off > 0; off >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, off));
     if ((threadIdx.x & 31) == 0) atomicMax(plane_max + plane, enc_ord(mx));
@@ -307,37 +323,93 @@ __device__ __forceinline__ void uf_union(int *P, int a, int b) {
     }
 }
 
-__global__ void uf_init(const float *__restrict__ w, int *__restrict__ P, size_t per_plane, int planes) {
-    const size_t total = per_plane * planes;
-    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
-        const size_t local = i % per_plane;
-        P[i] = (w[i] != 0.0f) ? (int)local : -1;
+// With segment flags (seg: per plane, one byte per 128 pixels, 0 when every pixel
+// of the segment is zero), P of an empty segment is neither written nor read by any
+// labelling or extraction kernel: those pixels are background.
+__device__ __forceinline__ bool seg_live(const unsigned char *seg, size_t local) {
+    return !seg || __ldg(seg + (local >> 7)) != 0;
+}
+
+// One plane per blockIdx.y, four pixels per step (float4 of w, int4 of P); a warp's
+// 32 steps are one segment.
+__global__ void uf_init(const float *__restrict__ w, int *__restrict__ P, int per4,
+                        const unsigned char *__restrict__ seg_all) {
+    const size_t plane = blockIdx.y;
+    const float4 *w4 = reinterpret_cast<const float4 *>(w) + plane * per4;
+    int4 *P4 = reinterpret_cast<int4 *>(P) + plane * per4;
+    const unsigned char *seg = seg_all ? seg_all + plane * ((per4 + 31) / 32) : nullptr;
+    for (int i4 = blockIdx.x * blockDim.x + threadIdx.x; i4 < per4; i4 += gridDim.x * blockDim.x) {
+        if (seg && !__ldg(seg + (i4 >> 5))) continue;
+        const float4 v = __ldg(w4 + i4);
+        const int b = 4 * i4;
+        P4[i4] = make_int4(v.x != 0.0f ? b : -1, v.y != 0.0f ? b + 1 : -1, v.z != 0.0f ? b + 2 : -1,
+                           v.w != 0.0f ? b + 3 : -1);
     }
 }
 
-__global__ void uf_merge(int *__restrict__ Pall, int ny, int nx) {
+// Scalar forms for any plane size and alignment (msn_label): one pixel per step.
+__global__ void uf_init_scalar(const float *__restrict__ w, int *__restrict__ P, int per) {
+    const size_t plane = blockIdx.y;
+    const float *wp = w + plane * per;
+    int *Pp = P + plane * per;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < per; i += gridDim.x * blockDim.x)
+        Pp[i] = (wp[i] != 0.0f) ? i : -1;
+}
+
+__global__ void uf_compress_scalar(int *__restrict__ P, int per) {
+    int *Pp = P + (size_t)blockIdx.y * per;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < per; i += gridDim.x * blockDim.x)
+        if (Pp[i] >= 0) Pp[i] = uf_find(Pp, i);
+}
+
+// Unions of each foreground pixel e with its earlier 8-neighbours a = (y-1, x-1),
+// b = (y-1, x), c = (y-1, x+1), d = (y, x-1), by the decision tree of Wu, Otoo and
+// Suzuki ("Optimizing two-pass connected-component labeling algorithms", 2009):
+// when b is foreground, a, c and d are already joined to it through other pixels'
+// unions, so e joins b alone; otherwise e joins c and, since c is not adjacent to
+// a or d, also a or else d; with neither b nor c, e joins a or else d. The
+// transitive closure is 8-connectivity, as with all four unions, and the roots
+// (smallest index of each component, by the atomicMin hooking) are unchanged.
+__global__ void uf_merge(int *__restrict__ Pall, int ny, int nx, const unsigned char *__restrict__ seg_all) {
     const int plane = blockIdx.y;
     int *P = Pall + (size_t)plane * ny * nx;
     const int total = ny * nx;
+    const unsigned char *seg = seg_all ? seg_all + (size_t)plane * ((total + 127) / 128) : nullptr;
+    // a foreground pixel: in a live segment and labelled
+    auto fg = [&](int j) { return seg_live(seg, (size_t)j) && __ldcg(P + j) >= 0; };
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
-        if (__ldcg(P + i) < 0) continue;
+        if (!fg(i)) continue;
         const int y = i / nx, x = i - y * nx;
-        if (x > 0 && __ldcg(P + i - 1) >= 0) uf_union(P, i, i - 1);
-        if (y > 0) {
-            const int up = i - nx;
-            if (x > 0 && __ldcg(P + up - 1) >= 0) uf_union(P, i, up - 1);
-            if (__ldcg(P + up) >= 0) uf_union(P, i, up);
-            if (x + 1 < nx && __ldcg(P + up + 1) >= 0) uf_union(P, i, up + 1);
+        const int up = i - nx;
+        const bool b = y > 0 && fg(up);
+        if (b) {
+            uf_union(P, i, up);
+            continue;
         }
+        const bool c = y > 0 && x + 1 < nx && fg(up + 1);
+        const bool a = y > 0 && x > 0 && fg(up - 1);
+        const bool d = x > 0 && fg(i - 1);
+        if (c) uf_union(P, i, up + 1);
+        if (a)
+            uf_union(P, i, up - 1);
+        else if (d)
+            uf_union(P, i, i - 1);
     }
 }
 
-__global__ void uf_compress(int *__restrict__ Pall, size_t per_plane, int planes) {
-    const size_t total = per_plane * planes;
-    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
-        int *P = Pall + (i / per_plane) * per_plane;
-        const int local = (int)(i % per_plane);
-        if (P[local] >= 0) P[local] = uf_find(P, local);
+__global__ void uf_compress(int *__restrict__ P, int per4, const unsigned char *__restrict__ seg_all) {
+    const size_t plane = blockIdx.y;
+    int *Pp = P + plane * per4 * 4;
+    const unsigned char *seg = seg_all ? seg_all + plane * ((per4 + 31) / 32) : nullptr;
+    for (int i4 = blockIdx.x * blockDim.x + threadIdx.x; i4 < per4; i4 += gridDim.x * blockDim.x) {
+        if (seg && !__ldg(seg + (i4 >> 5))) continue;
+        int4 v = reinterpret_cast<const int4 *>(Pp)[i4];
+        if ((v.x & v.y & v.z & v.w) < 0) continue;  // all four background
+        if (v.x >= 0) v.x = uf_find(Pp, v.x);
+        if (v.y >= 0) v.y = uf_find(Pp, v.y);
+        if (v.z >= 0) v.z = uf_find(Pp, v.z);
+        if (v.w >= 0) v.w = uf_find(Pp, v.w);
+        reinterpret_cast<int4 *>(Pp)[i4] = v;
     }
 }
 
@@ -346,9 +418,10 @@ __global__ void uf_compress(int *__restrict__ Pall, size_t per_plane, int planes
 // ---------------------------------------------------------------------------
 __global__ void extract_mark(const float *__restrict__ w, const int *__restrict__ P, const float *__restrict__ mask_above,
                              const int *__restrict__ maxima_enc, int plane, float tolerance, int neg_comp,
-                             unsigned char *__restrict__ keep, int n) {
+                             unsigned char *__restrict__ keep, int n, const unsigned char *__restrict__ seg) {
     const float thr = __fmul_rn(tolerance, dec_ord(maxima_enc[plane]));
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        if (!seg_live(seg, (size_t)i)) continue;
         const int root = P[i];
         if (root < 0) continue;
         const float v = neg_comp ? fabsf(w[i]) : w[i];
@@ -358,10 +431,17 @@ __global__ void extract_mark(const float *__restrict__ w, const int *__restrict_
     }
 }
 
+// A pixel of an empty segment is background (mask 0) without reading its label;
+// extracted is still the product 0 * w, which keeps the sign of a zero w.
 __global__ void extract_apply(const float *__restrict__ w, const int *__restrict__ P,
                               const unsigned char *__restrict__ keep, float *__restrict__ mask,
-                              float *__restrict__ extracted, int n) {
+                              float *__restrict__ extracted, int n, const unsigned char *__restrict__ seg) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        if (!seg_live(seg, (size_t)i)) {
+            mask[i] = 0.0f;
+            if (extracted) extracted[i] = __fmul_rn(0.0f, w[i]);
+            continue;
+        }
         const int root = P[i];
         const float m = (root >= 0 && keep[root]) ? 1.0f : 0.0f;
         mask[i] = m;
@@ -462,14 +542,27 @@ int grid_for(size_t n, int threads, int cap = 152 * 16) {
 
 size_t a256(size_t b) { return (b + 255) & ~(size_t)255; }
 
-int launch_labelling(const float *w, int planes, int ny, int nx, int *P, cudaStream_t st) {
+// seg (may be null): segment flags of every plane (plane_max_kernel).
+int launch_labelling(const float *w, int planes, int ny, int nx, int *P, cudaStream_t st,
+                     const unsigned char *seg = nullptr) {
     const size_t per = (size_t)ny * nx;
-    uf_init<<<grid_for(per * planes, 256), 256, 0, st>>>(w, P, per, planes);
+    // four pixels per step where the planes allow it (the segment flags need it)
+    const bool vec = per % 4 == 0 && aligned16(w) && aligned16(P);
+    if (seg && !vec) return set_error(MSN_ERR_INVALID, "labelling: segment flags need 16-byte aligned planes");
+    const int per4 = (int)(per / 4);
+    const int gx = grid_for(vec ? (size_t)per4 : per, 256, 8 * 152 / planes + 8);
+    if (vec)
+        uf_init<<<dim3(gx, planes), 256, 0, st>>>(w, P, per4, seg);
+    else
+        uf_init_scalar<<<dim3(gx, planes), 256, 0, st>>>(w, P, (int)per);
     MSN_TRY(check_launch("uf_init"));
     dim3 g(grid_for(per, 256, 152 * 8), planes);
-    uf_merge<<<g, 256, 0, st>>>(P, ny, nx);
+    uf_merge<<<g, 256, 0, st>>>(P, ny, nx, seg);
     MSN_TRY(check_launch("uf_merge"));
-    uf_compress<<<grid_for(per * planes, 256), 256, 0, st>>>(P, per, planes);
+    if (vec)
+        uf_compress<<<dim3(gx, planes), 256, 0, st>>>(P, per4, seg);
+    else
+        uf_compress_scalar<<<dim3(gx, planes), 256, 0, st>>>(P, (int)per);
     return check_launch("uf_compress");
 }
 
@@ -479,9 +572,11 @@ int launch_labelling(const float *w, int planes, int ny, int nx, int *P, cudaStr
 size_t mad_workspace(int planes) {
     return a256((size_t)planes * 2 * kHistBins * sizeof(unsigned)) + a256((size_t)planes * sizeof(SelectState));
 }
+size_t seg_bytes(int ny, int nx) { return ((size_t)ny * nx + 127) / 128; }
 size_t extract_workspace(int planes, int ny, int nx) {
     const size_t per = (size_t)ny * nx;
-    return a256(per * planes * sizeof(int)) + a256(per * planes) + a256((size_t)planes * sizeof(int));
+    return a256(per * planes * sizeof(int)) + a256(per * planes) + a256((size_t)planes * sizeof(int)) +
+           a256(seg_bytes(ny, nx) * planes);
 }
 size_t label_workspace(int ny, int nx) {
     const size_t per = (size_t)ny * nx;
@@ -535,20 +630,25 @@ int extraction_impl(const float *w, int planes, int ny, int nx, float tolerance,
     int *P = (int *)work;
     unsigned char *keep = (unsigned char *)work + a256(per * planes * sizeof(int));
     int *maxima = (int *)((char *)keep + a256(per * planes));
+    // per plane, one flag per 128 pixels: labelling and extraction skip empty segments
+    unsigned char *seg = (unsigned char *)maxima + a256((size_t)planes * sizeof(int));
+    const size_t nseg = seg_bytes(ny, nx);
     init_max<<<(planes + 127) / 128, 128, 0, st>>>(maxima, planes);
     MSN_TRY(check_launch("init_max"));
     plane_max_kernel<<<dim3(grid_for(per / 4, 256, 4 * 152 / planes + 8), planes), 256, 0, st>>>(w, per / 4, neg_comp,
-                                                                                                 maxima);
+                                                                                                 maxima, seg);
     MSN_TRY(check_launch("plane_max"));
-    MSN_TRY(launch_labelling(w, planes, ny, nx, P, st));
+    MSN_TRY(launch_labelling(w, planes, ny, nx, P, st, seg));
     MSN_TRY(check_cuda(cudaMemsetAsync(keep, 0, per * planes, st), "keep memset"));
     for (int i = planes - 1; i >= 0; --i) {
         const size_t off = (size_t)i * per;
         extract_mark<<<grid_for(per, 256), 256, 0, st>>>(w + off, P + off, i == planes - 1 ? nullptr : mask + off + per,
-                                                         maxima, i, tolerance, neg_comp, keep + off, (int)per);
+                                                         maxima, i, tolerance, neg_comp, keep + off, (int)per,
+                                                         seg + (size_t)i * nseg);
         MSN_TRY(check_launch("extract_mark"));
         extract_apply<<<grid_for(per, 256), 256, 0, st>>>(w + off, P + off, keep + off, mask + off,
-                                                          extracted ? extracted + off : nullptr, (int)per);
+                                                          extracted ? extracted + off : nullptr, (int)per,
+                                                          seg + (size_t)i * nseg);
         MSN_TRY(check_launch("extract_apply"));
     }
     return MSN_OK;
@@ -632,6 +732,8 @@ extern "C" int msn_source_extraction(const float *d_w, int planes, int ny, int n
     static const char *fn = "msn_source_extraction";
     MSN_TRY(validate_planes(planes, ny, nx, fn));
     if (!d_w || !d_mask) return set_error(MSN_ERR_INVALID, "%s: null pointer", fn);
+    if (!aligned16(d_w) || !aligned16(d_work))
+        return set_error(MSN_ERR_INVALID, "%s: planes and workspace must be 16-byte aligned", fn);
     if (!d_work || work_bytes < extract_workspace(planes, ny, nx))
         return set_error(MSN_ERR_WORKSPACE, "%s: workspace too small", fn);
     return extraction_impl(d_w, planes, ny, nx, tolerance, neg_comp, d_mask, d_extracted, d_work, as_stream(stream));
@@ -641,15 +743,16 @@ extern "C" int msn_plane_max(const float *d_w, int planes, size_t per_plane, int
                              size_t work_bytes, void *stream) {
     clear_error();
     static const char *fn = "msn_plane_max";
-    if (!d_w || !d_out || planes <= 0 || per_plane == 0 || per_plane % 4)
-        return set_error(MSN_ERR_INVALID, "%s: bad arguments (plane size must be a positive multiple of 4)", fn);
+    if (!d_w || !d_out || planes <= 0 || per_plane == 0 || per_plane % 4 || !aligned16(d_w))
+        return set_error(MSN_ERR_INVALID,
+                         "%s: bad arguments (plane size a positive multiple of 4, planes 16-byte aligned)", fn);
     if (!d_work || work_bytes < (size_t)planes * sizeof(int)) return set_error(MSN_ERR_WORKSPACE, "%s: workspace", fn);
     cudaStream_t st = as_stream(stream);
     int *enc = (int *)d_work;
     init_max<<<(planes + 127) / 128, 128, 0, st>>>(enc, planes);
     MSN_TRY(check_launch("init_max"));
     plane_max_kernel<<<dim3(grid_for(per_plane / 4, 256, 4 * 152 / planes + 8), planes), 256, 0, st>>>(
-        d_w, per_plane / 4, use_abs, enc);
+        d_w, per_plane / 4, use_abs, enc, nullptr);
     MSN_TRY(check_launch("plane_max"));
     decode_max<<<(planes + 127) / 128, 128, 0, st>>>(enc, d_out, planes);
     return check_launch("decode_max");
