@@ -534,6 +534,33 @@ __global__ void gather_labels(const int *__restrict__ P, const int *__restrict__
     }
 }
 
+// One step down the scales: extract_apply of plane hi, then extract_mark of plane
+// lo = hi - 1 against the mask just formed at the same pixel (what extract_mark
+// would read back from mask_hi), so each plane pair takes one pass.
+__global__ void extract_step(const float *__restrict__ w_hi, const int *__restrict__ P_hi,
+                             const unsigned char *__restrict__ keep_hi, float *__restrict__ mask_hi,
+                             float *__restrict__ ext_hi, const unsigned char *__restrict__ seg_hi,
+                             const float *__restrict__ w_lo, const int *__restrict__ P_lo,
+                             const unsigned char *__restrict__ seg_lo, const int *__restrict__ maxima_enc, int lo_plane,
+                             float tolerance, int neg_comp, unsigned char *__restrict__ keep_lo, int n) {
+    const float thr = __fmul_rn(tolerance, dec_ord(maxima_enc[lo_plane]));
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        float m = 0.0f;
+        if (seg_live(seg_hi, (size_t)i)) {
+            const int root = P_hi[i];
+            m = (root >= 0 && keep_hi[root]) ? 1.0f : 0.0f;
+        }
+        mask_hi[i] = m;
+        if (ext_hi) ext_hi[i] = __fmul_rn(m, w_hi[i]);
+        if (m == 0.0f || !seg_live(seg_lo, (size_t)i)) continue;
+        const int root = P_lo[i];
+        if (root < 0) continue;
+        const float v = neg_comp ? fabsf(w_lo[i]) : w_lo[i];
+        if (!(v >= thr)) continue;
+        keep_lo[root] = 1;
+    }
+}
+
 int grid_for(size_t n, int threads, int cap = 152 * 16) {
     size_t g = (n + threads - 1) / threads;
     if (g > (size_t)cap) g = cap;
@@ -640,18 +667,23 @@ int extraction_impl(const float *w, int planes, int ny, int nx, float tolerance,
     MSN_TRY(check_launch("plane_max"));
     MSN_TRY(launch_labelling(w, planes, ny, nx, P, st, seg));
     MSN_TRY(check_cuda(cudaMemsetAsync(keep, 0, per * planes, st), "keep memset"));
-    for (int i = planes - 1; i >= 0; --i) {
-        const size_t off = (size_t)i * per;
-        extract_mark<<<grid_for(per, 256), 256, 0, st>>>(w + off, P + off, i == planes - 1 ? nullptr : mask + off + per,
-                                                         maxima, i, tolerance, neg_comp, keep + off, (int)per,
-                                                         seg + (size_t)i * nseg);
-        MSN_TRY(check_launch("extract_mark"));
-        extract_apply<<<grid_for(per, 256), 256, 0, st>>>(w + off, P + off, keep + off, mask + off,
-                                                          extracted ? extracted + off : nullptr, (int)per,
-                                                          seg + (size_t)i * nseg);
-        MSN_TRY(check_launch("extract_apply"));
+    // top-down over the scales: mark the top plane, then per step apply plane i + 1 and mark
+    // plane i, then apply plane 0
+    const int top = planes - 1;
+    const size_t ot = (size_t)top * per;
+    extract_mark<<<grid_for(per, 256), 256, 0, st>>>(w + ot, P + ot, nullptr, maxima, top, tolerance, neg_comp,
+                                                     keep + ot, (int)per, seg + (size_t)top * nseg);
+    MSN_TRY(check_launch("extract_mark"));
+    for (int i = top - 1; i >= 0; --i) {
+        const size_t hi = (size_t)(i + 1) * per, lo = (size_t)i * per;
+        extract_step<<<grid_for(per, 256), 256, 0, st>>>(w + hi, P + hi, keep + hi, mask + hi,
+                                                         extracted ? extracted + hi : nullptr, seg + (size_t)(i + 1) * nseg,
+                                                         w + lo, P + lo, seg + (size_t)i * nseg, maxima, i, tolerance,
+                                                         neg_comp, keep + lo, (int)per);
+        MSN_TRY(check_launch("extract_step"));
     }
-    return MSN_OK;
+    extract_apply<<<grid_for(per, 256), 256, 0, st>>>(w, P, keep, mask, extracted, (int)per, seg);
+    return check_launch("extract_apply");
 }
 
 int label_impl(const float *img, int ny, int nx, int *labels, int *count, void *work, cudaStream_t st) {
