@@ -651,7 +651,7 @@ int dual_reduce(const float *a, const float *b, const float *c, const float *d, 
 
 int dot_rows(const float *a, const float *b, size_t n, RowSupport sup, double *out, void *work, size_t work_bytes,
              cudaStream_t st) {
-    if (!a || !b || !out || !work || work_bytes < kPartialBytes || !sup.rows || sup.cols4 == 0)
+    if (!a || !b || !out || !work || work_bytes < kPartialBytes || sup.cols4 == 0)
         return set_error(MSN_ERR_INVALID, "dot_rows: bad arguments");
     return dual_reduce(a, b, nullptr, nullptr, n, false, out, (double *)work, st, sup);
 }

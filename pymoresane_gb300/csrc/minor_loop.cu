@@ -260,7 +260,10 @@ int build_graph(Engine *e, const msn_minor_args *a, CacheEntry *ce) {
     if (a->enforce_positivity)
         MSN_TRY(check_cuda(cudaGraphConditionalHandleCreate(&if_h, body, 0u, 0u), "positivity handle"));
     long long branch_kernels = 0;
-    const RowSupport sup{a->rec_rows, (unsigned)(a->n / 4)};
+    // float4 elements never straddle rows when n is a multiple of 4 (the IUWT requires it);
+    // otherwise the vector passes stay dense
+    const RowSupport sup = (a->n % 4 == 0 && a->n >= 4) ? RowSupport{a->rec_rows, (unsigned)(a->n / 4)}
+                                                        : RowSupport{nullptr, 1u};
     MSN_TRY(capture_into(e->cs[1], body, &ce->body_kernels, [&](cudaStream_t st) -> int {
         // the body's kernels may each launch while their predecessor finishes (launch_k)
         const PdlScope pdl(tune_value(kKnobGraphPdl) != 0);
