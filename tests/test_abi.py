@@ -111,3 +111,17 @@ def test_engine_entry_points_reject_null_engine(lib):
     with pytest.raises(ValueError, match="null engine"):
         _native.call("msn_moresane_run", None, ctypes.byref(margs), ctypes.byref(mres), None, 0, None, 0, None)
     assert _native.query("msn_minor_engine_destroy", None) == 0
+
+
+def test_float4_entry_points_reject_unaligned_planes(lib):
+    """Argument checks that run before any CUDA call: the plane passes read float4, so planes that
+    are not 16-byte aligned are refused instead of faulting (addresses are never dereferenced)."""
+    bad = ctypes.c_void_p(0x1008)   # 8 bytes past a 16-byte boundary
+    good = ctypes.c_void_p(0x2000)
+    with pytest.raises(ValueError, match="16-byte aligned"):
+        _native.call("msn_source_extraction", bad, 2, 64, 64, ctypes.c_float(0.75), 0, good, None, good, 1 << 30,
+                     None)
+    with pytest.raises(ValueError, match="16-byte aligned"):
+        _native.call("msn_plane_max", bad, 2, 64 * 64, 0, good, good, 1 << 20, None)
+    with pytest.raises(ValueError, match="null row flags"):
+        _native.call("msn_fft_convolve_rows", good, 2048, 4096, good, good, 1, None, good, 1 << 30, None)
