@@ -282,11 +282,11 @@ def deconv_trajectory(fallback):
     return tuple(fallback), "this implementation's complete run of this problem (reference run not recorded)"
 
 
-def run_deconv(args, rank, world, dist):
+def run_deconv(args, rank, world, dist, problem=None):
     import torch
 
     from pymoresane_gb300.main import DataImage, Deconvolver
-    dirty_h, psf_h = deconv_problem(rank)
+    dirty_h, psf_h = problem if problem is not None else deconv_problem(rank)
     dirty = torch.from_numpy(dirty_h).cuda()
     psf = torch.from_numpy(psf_h).cuda()
 
@@ -658,10 +658,21 @@ def main():
             dist.destroy_process_group()
         return
 
-    # the project's autotuner picks this device's launch parameters before anything is timed
+    # the project's autotuner picks this device's launch parameters before anything is timed;
+    # the a trous CTA size on a deconvolution of the benchmarked problem bounded to 3 major iterations
     from pymoresane_gb300 import tune
-    tuned = tune.autotune(n=2048, reps=5)["values"] if not args.no_tune else tune.current()
-    res = run_deconv(args, rank, world, dist)
+    problem = deconv_problem(rank)
+    if args.no_tune:
+        tuned = tune.current()
+    else:
+        import torch
+
+        from pymoresane_gb300.main import Deconvolver
+        d_dev, p_dev = torch.from_numpy(problem[0]).cuda(), torch.from_numpy(problem[1]).cuda()
+        short = dict(DECONV_KW, major_loop_miter=3)
+        tuned = tune.autotune(n=2048, reps=5, workload=lambda: Deconvolver(p_dev).moresane(d_dev, **short))["values"]
+        del d_dev, p_dev
+    res = run_deconv(args, rank, world, dist, problem)
     served = None
     if args.served_jobs > 0 and args.driver == "native":
         served = run_served_2048(args, res["dirty"], res["psf"], res["model"])

@@ -10,7 +10,7 @@ speed, and the best values depend on the device.
 
 ``autotune()`` times the candidates of each parameter on the real operation
 (CUDA events on the current stream, the median of several runs after a
-warm-up), keeps the fastest, sets it in the library and stores the choice in a
+warm-up; the a trous CTA size on a short deconvolution when the caller gives one), keeps the fastest, sets it in the library and stores the choice in a
 JSON cache keyed by the device (name, SM count, compute capability).
 ``ensure_applied()`` loads the cache once per process and sets the cached
 values; the deconvolution driver calls it, so a tuned device keeps its choices
@@ -134,9 +134,15 @@ def _timer(fn, reps, warmup=2):
     return measure
 
 
-def autotune(n=2048, reps=10, path=None, save=True):
+def autotune(n=2048, reps=10, path=None, save=True, workload=None):
     """Tunes every parameter on an n x n problem (convolution with a 2n x 2n PSF spectrum,
     decomposition + recomposition with log2(n) - 4 scales) and caches the result.
+
+    workload (optional): a callable that runs a short piece of the real computation, such as a
+    deconvolution bounded to a few major iterations. The a trous CTA size is then timed on it
+    instead of on the dense decomposition + recomposition: a deconvolution's passes are masked
+    and skip rows, and on GB300 they favour a different CTA size (a 2048^2 deconvolution took
+    497.6 ms with 256 threads against 506.4 ms with the 128 the dense passes favour).
 
     Returns {"device": key, "values": {...}, "times_s": {...}}.
     """
@@ -175,7 +181,7 @@ def autotune(n=2048, reps=10, path=None, save=True):
             continue
         if name == ("iuwt_threads_wide" if n <= 2048 else "iuwt_threads"):
             continue
-        op = iuwt if name.startswith("iuwt_") else conv
+        op = (workload or iuwt) if name.startswith("iuwt_") else conv
         best, t = choose(name, CANDIDATES[name], _timer(op, reps))
         times[name] = {str(k): v for k, v in t.items()}
         tuned[name] = best
