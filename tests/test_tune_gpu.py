@@ -45,3 +45,23 @@ def test_autotune_choices_do_not_change_results(cuda, tmp_path):
             assert torch.equal(dev.iuwt_decompose(xw, 5, 0)[0], ww_ref)
     finally:
         tune.reset()
+
+
+def test_autotune_times_the_cta_size_on_a_given_workload(cuda, tmp_path):
+    # with workload=, the a trous CTA size is timed on the caller's operation (every candidate
+    # runs it); the convolution parameters still on the convolution
+    rng = np.random.default_rng(5)
+    x = torch.from_numpy(rng.standard_normal((2048, 2048)).astype(np.float32)).cuda()
+    calls = []
+
+    def work():
+        calls.append(tune.get("iuwt_threads"))
+        dev.iuwt_decompose(x, 4, 0)
+
+    tune.reset()
+    try:
+        res = tune.autotune(n=2048, reps=1, path=str(tmp_path / "tune.json"), workload=work)
+        assert "iuwt_threads" in res["tuned"] and "fft_four_step" in res["tuned"]
+        assert sorted(set(calls)) == sorted(tune.CANDIDATES["iuwt_threads"])
+    finally:
+        tune.reset()
