@@ -680,18 +680,6 @@ int cg_step_snr_rows(const float *x, const float *p, const float *r, const float
     return go(cg_step_snr<FF>);
 }
 
-int cg_step_rows(const float *x, const float *p, const float *r, const float *ap, double *scal, float *xn, float *rn,
-                 size_t n, RowSupport sup, void *work, size_t work_bytes, cudaStream_t st) {
-    if (!x || !p || !r || !ap || !scal || !xn || !rn || !work || work_bytes < kPartialBytes || sup.cols4 == 0)
-        return set_error(MSN_ERR_INVALID, "cg_step_rows: bad arguments");
-    if (n % 4 || !aligned16(x) || !aligned16(p) || !aligned16(r) || !aligned16(ap) || !aligned16(xn) ||
-        !aligned16(rn))
-        return set_error(MSN_ERR_INVALID, "cg_step_rows: length must be a multiple of 4, pointers 16-byte aligned");
-    MSN_RED_LAUNCH(cg_step, kRedGrid, kRedThreads, st, (const float4 *)x, (const float4 *)p, (const float4 *)r,
-                   (const float4 *)ap, scal, (float4 *)xn, (float4 *)rn, n / 4, (double *)work, sup);
-    return check_launch("cg_step");
-}
-
 }  // namespace msn
 
 using namespace msn;

@@ -95,12 +95,9 @@ struct RowSupport {
 int fft_convolve_rows(const float *d_x, int n, int m, const void *d_spec, float *d_out, int linear, void *d_work,
                       size_t work_bytes, const unsigned char *rows, cudaStream_t st);
 
-// cg.cu entry points of the graph minor loop with a row support: out[0] = a . b,
-// and the conjugate-gradient step of msn_cg_step.
+// cg.cu: out[0] = a . b over the rows of a row support (the graph minor loop's p.Ap).
 int dot_rows(const float *a, const float *b, size_t n, RowSupport sup, double *out, void *work, size_t work_bytes,
              cudaStream_t st);
-int cg_step_rows(const float *x, const float *p, const float *r, const float *ap, double *scal, float *xn, float *rn,
-                 size_t n, RowSupport sup, void *work, size_t work_bytes, cudaStream_t st);
 
 inline cudaStream_t as_stream(void *s) { return reinterpret_cast<cudaStream_t>(s); }
 
