@@ -56,9 +56,9 @@ __device__ __forceinline__ FF shfl_xor(FF v, int off) {
     return r;
 }
 
-// Accumulation type of the reductions within a CTA: FF (float-float, the
-// default), double (msn_set_reduction_precision(64)) or float (the plain float32
-// variant, 32); the sum across CTAs is float64 except in the float32 variant.
+// Accumulation type of the reductions within a CTA: double (the default,
+// msn_set_reduction_precision(64)), FF (float-float, 48) or float (the plain
+// float32 variant, 32); the sum across CTAs is float64 except in the float32 variant.
 template <class T>
 __device__ __forceinline__ T block_sum(T v) {
     __shared__ T sh[32];
