@@ -16,11 +16,14 @@
 //   p = rn + beta p; r = rn; x = xn unless the stop rule discards xn
 //
 // so the host launches one graph per minor loop and reads one small state
-// block back. The stop rules run on the device (minor_control) and set the
+// block back. The stop rules run on the device (minor_control_apply) and set the
 // WHILE condition with cudaGraphSetConditional; the positivity branch is an IF
-// node set the same way. Each body operation is the library's own C-ABI entry
-// point, captured on a private stream, so the arithmetic is identical to the
-// step-by-step path. Instantiated graphs are cached per engine and keyed by the
+// node set the same way. Without positivity, the lines from xn = x + alpha p
+// to rn.rn and beta are one launch (cg_step_snr, whose last CTA applies the stop
+// rules), and every vector pass skips the rows outside the recomposition's
+// support, where all vectors are zero. The body's operations have the arithmetic
+// of the library's step entry points (the host-driven loop gives the same model
+// bit for bit). Instantiated graphs are cached per engine and keyed by the
 // full argument block (buffers, sizes, scales), so a deconvolution that keeps
 // its buffers re-uses them across minor loops.
 #include <cmath>
