@@ -28,6 +28,7 @@ import torch
 
 from . import _native
 from . import device as dev
+from . import tune
 
 F32 = 4
 C64 = 8
@@ -186,6 +187,12 @@ class DeconvolutionExecutor:
         self._seq = itertools.count()
         self._cv = threading.Condition()
         self._closed = False
+        # this device's tuned values first, then (with several workers) the values that favour
+        # concurrent deconvolutions, restored when the executor shuts down
+        tune.ensure_applied()
+        self._concurrent = workers > 1
+        if self._concurrent:
+            tune.enter_concurrent()
         self._threads = [threading.Thread(target=self._worker, args=(i,), daemon=True) for i in range(workers)]
         for t in self._threads:
             t.start()
@@ -209,10 +216,14 @@ class DeconvolutionExecutor:
 
     def shutdown(self):
         with self._cv:
+            if self._closed:
+                return
             self._closed = True
             self._cv.notify_all()
         for t in self._threads:
             t.join()
+        if self._concurrent:
+            tune.leave_concurrent()
 
     def __enter__(self):
         return self

@@ -44,3 +44,16 @@ def test_cache_round_trip_and_apply(tmp_path, monkeypatch):
     assert tune.get("fft_four_step") == 0 and tune.get("iuwt_threads") == 64
     assert tune.ensure_applied(path) is None          # once per process
     assert tune.load_cache(str(tmp_path / "missing.json")) == {}
+
+
+def test_concurrent_values_nest_and_restore():
+    # executors with several workers set the concurrency values while any of them runs; the
+    # last to stop restores what was there before
+    tune.set_values({"iuwt_threads": 256})
+    tune.enter_concurrent()
+    assert tune.get("iuwt_threads") == tune.CONCURRENT["iuwt_threads"]
+    tune.enter_concurrent()
+    tune.leave_concurrent()
+    assert tune.get("iuwt_threads") == tune.CONCURRENT["iuwt_threads"]
+    tune.leave_concurrent()
+    assert tune.get("iuwt_threads") == 256
