@@ -200,10 +200,12 @@ def autotune(n=2048, reps=10, path=None, save=True, workload=None):
 
 
 # Launch parameters for concurrent deconvolutions on one GPU (DeconvolutionExecutor with
-# more than one worker). Smaller a trous CTAs interleave better across streams: 8 concurrent
-# 2048^2 deconvolutions ran at 2.39 deconv/s with 128 threads against 2.25 with 256 (GB300,
-# same process), while a single deconvolution is faster with 256.
-CONCURRENT = {"iuwt_threads": 128}
+# more than one worker). Smaller a trous CTAs and fewer resident four-step row-transform CTAs
+# interleave better across streams: 8 concurrent 2048^2 deconvolutions ran at 2.39 deconv/s
+# with 128-thread a trous CTAs against 2.25 with 256, and at 2.54 against 2.38 with the two
+# row kernels capped at 2 CTAs per SM (GB300, same process); a single deconvolution is faster
+# with the tuned values.
+CONCURRENT = {"iuwt_threads": 128, "fft_sq_fwd_ctas": 2, "fft_sq_inv_ctas": 2}
 _conc_lock = threading.Lock()
 _conc_depth = 0
 _conc_saved = None
