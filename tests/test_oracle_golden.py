@@ -5,6 +5,7 @@ which runs the reference PyMORESANE ('ser', 'mp', 'cpu' paths) on seeded
 inputs. The oracle restatement must reproduce them.
 """
 import os
+import sys
 
 import numpy as np
 import pytest
@@ -118,3 +119,28 @@ def test_moresane_oracle_bit_exact(name):
     assert o.model.dtype == g[f"{name}_model"].dtype
     assert np.array_equal(o.model, g[f"{name}_model"])
     assert np.array_equal(o.residual, g[f"{name}_residual"])
+
+
+@pytest.mark.parametrize("name,majors,minors", [("baseline_512", 62, None), ("baseline_2048_m3", 3, None),
+                                                ("baseline_2048_full", 90, 1595)])
+def test_baseline_fixtures_hold_the_reference_trajectory(name, majors, minors):
+    # the reference's own runs of the benchmark problems: the parsed INFO log gives the major count
+    # and the minor-iteration total stored beside it (bench.py scales its CPU baseline by the 2048^2
+    # full run's); every minor loop of a major iteration is counted
+    path = os.path.join(GOLDEN, name + ".npz")
+    if not os.path.exists(path):
+        pytest.skip(f"{name}.npz not generated")
+    g = np.load(path)
+    sys.path.insert(0, GOLDEN)
+    import cases as mg
+    recs = mg.parse_major_log([str(s) for s in g["log"]])
+    assert len(recs) == int(g["major"]) == majors
+    total = sum(sum(r["minor"]) for r in recs)
+    assert total == int(g["minor_total"])
+    if minors is not None:
+        assert total == minors
+    model = g["model"] if "model" in g else None
+    if model is None:
+        model = np.zeros(int(np.prod(g["model_shape"])), np.float32)
+        model[g["model_idx"]] = g["model_val"]
+    assert np.isfinite(model).all() and np.count_nonzero(model) > 0
